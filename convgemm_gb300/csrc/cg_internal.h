@@ -1,0 +1,37 @@
+// Internal host-side interfaces between the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "../../include/convgemm_gpu.h"
+
+struct cg_shape {
+    int b, h, w, c, kn, kh, kw;
+    int vpad, hpad, vstride, hstride, vdil, hdil;
+};
+
+static inline cg_shape cg_from_public(const convgemm_shape_t &s) {
+    cg_shape r = {s.b, s.h, s.w, s.c, s.kn, s.kh, s.kw, s.vpad, s.hpad, s.vstride, s.hstride, s.vdil, s.hdil};
+    return r;
+}
+
+struct cg_epi {
+    const float *bias, *mean, *inv_std, *gamma, *beta;
+    int relu;
+};
+
+// Records an error for convgemm_get_last_error(); returns the status.
+convgemm_status_t cg_set_error(convgemm_status_t st, const char *fmt, ...);
+convgemm_status_t cg_cuda_check(cudaError_t e, const char *what);
+
+// FP32 launchers (cg_fp32.cu).  Inputs are validated by the caller.
+cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float *x, float *y,
+                        const cg_epi &e, cudaStream_t st);
+size_t cg_fp32_wgrad_ws_bytes(const cg_shape &s);
+cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const float *x, float *dw,
+                          float *ws, cudaStream_t st);
+cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const float *dy, float *dx,
+                          int accumulate, cudaStream_t st);
+
+// Device error word (set by bounded waits); defined in cg_runtime.cu.
+int *cg_device_error_word();

@@ -1,0 +1,95 @@
+/*
+ * convGemm GB300 extended interface: explicit streams, device pointers,
+ * status codes, caller-provided workspaces and the tensor-core precision forms.
+ *
+ * The reference has no counterpart for most of this file; each function says
+ * which reference entry point it generalises.  All pointers are DEVICE
+ * pointers; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * Nothing here synchronises the stream unless it says so.
+ */
+#ifndef CONVGEMM_GPU_H
+#define CONVGEMM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CONVGEMM_SUCCESS = 0,
+    CONVGEMM_ERROR_INVALID_VALUE = 1,  /* bad geometry, NULL pointer, bad enum */
+    CONVGEMM_ERROR_NOT_SUPPORTED = 2,  /* no kernel for this shape / form */
+    CONVGEMM_ERROR_CUDA = 3,           /* a CUDA runtime or driver call failed */
+    CONVGEMM_ERROR_ALLOC = 4,          /* a device or host allocation failed */
+    CONVGEMM_ERROR_TIMEOUT = 5,        /* a bounded device-side wait ran out */
+    CONVGEMM_ERROR_WORKSPACE = 6       /* caller workspace smaller than required */
+} convgemm_status_t;
+
+typedef enum { CONVGEMM_NHWC = 0, CONVGEMM_NCHW = 1 } convgemm_layout_t;
+
+/* One 2-D convolution.  Output size follows src/convGemm.c:60-61:
+ * ho = (h + 2*vpad - vdil*(kh-1) - 1)/vstride + 1 (same for wo). */
+typedef struct {
+    int b, h, w, c;      /* batch, input height, width, channels */
+    int kn, kh, kw;      /* output channels, filter height, width */
+    int vpad, hpad;      /* symmetric zero padding */
+    int vstride, hstride;
+    int vdil, hdil;
+} convgemm_shape_t;
+
+/* Per-output-channel epilogue of the forward pass (src/im2row_nhwc.c:269-285):
+ * v += bias; v = (v - mean)*inv_std; v = v*gamma + beta; v = max(v, 0).
+ * Any pointer may be NULL; batch-norm is on when mean is set (then inv_std,
+ * gamma and beta must be set too). */
+typedef struct {
+    const float *bias;
+    const float *mean;
+    const float *inv_std;
+    const float *gamma;
+    const float *beta;
+    int relu;
+} convgemm_epilogue_t;
+
+/* ---------------------------------------------------------------- errors */
+
+/* Status and message of the last failing call on this host thread. */
+convgemm_status_t convgemm_get_last_status(void);
+const char *convgemm_get_last_error(void);
+void convgemm_clear_error(void);
+/* Reads (and clears) the device-side error word that bounded waits set; it
+ * synchronises the stream first. */
+convgemm_status_t convgemm_check_device(void *stream);
+
+/* ------------------------------------------------------- FP32 plain form */
+
+/* sconvGemmNHWC/NCHW(trans='N') on device pointers (src/convGemm.c:65-70, 116-119). */
+convgemm_status_t convgemm_fwd_f32(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                   const float *weights, const float *x, float *y,
+                                   const convgemm_epilogue_t *epi, void *stream);
+
+/* Workspace of convgemm_wgrad_f32 in bytes (the per-KC-block partials that
+ * the fixed-order reduction sums). */
+size_t convgemm_wgrad_f32_workspace_size(const convgemm_shape_t *shape);
+
+/* sconvGemmNHWC/NCHW(trans='T') on device pointers (src/convGemm.c:71-76, 120-124):
+ * dw = dY x im2row(x)^T, overwritten; bit-reproducible run to run. */
+convgemm_status_t convgemm_wgrad_f32(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                     const float *dy, const float *x, float *dw,
+                                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* sconvGemmNHWC_back / sconvGemmNCHW_back on device pointers
+ * (src/convGemm.c:82-97, 130-146) in gather form (no col2im scatter, no
+ * atomics, deterministic).  accumulate != 0 adds into dx as the reference
+ * does; accumulate == 0 overwrites dx. */
+convgemm_status_t convgemm_dgrad_f32(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                     const float *weights, const float *dy, float *dx,
+                                     int accumulate, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CONVGEMM_GPU_H */

@@ -1,0 +1,82 @@
+"""CPU tests of the C ABI boundary: the library loads, exports every symbol the
+public headers declare, and rejects bad arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for hdr in ("convGemm.h", "convgemm_gpu.h"):
+        src = open(os.path.join(ROOT, "include", hdr)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", src, re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_reference_entry_points():
+    names = declared_functions()
+    for n in ("alloc_pack_buffs", "sconvGemmNHWC", "sconvGemmNHWC_back", "sconvGemmNCHW", "sconvGemmNCHW_back"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(cglib):
+    L = cglib.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_drop_in_header_compiles_as_c(tmp_path):
+    """convGemm.h is usable from plain C (it brings its own <stdbool.h>)."""
+    import subprocess
+    src = tmp_path / "t.c"
+    src.write_text('#include "convGemm.h"\nint main(void){float*a,*b;return alloc_pack_buffs(&a,&b);}\n')
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), "-c",
+                        str(src), "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_alloc_pack_buffs_needs_no_gpu(cglib):
+    rc, a, b = cglib.alloc_pack_buffs()
+    assert rc == 0 and a is None and b is None
+
+
+@pytest.mark.parametrize("bad", [
+    dict(b=0), dict(kh=9), dict(vstride=0), dict(hdil=0), dict(vpad=-1), dict(c=0),
+])
+def test_invalid_geometry_rejected_without_gpu(cglib, bad):
+    args = dict(b=1, h=5, w=5, c=3, kn=4, kh=3, kw=3, vpad=0, hpad=0, vstride=1, hstride=1, vdil=1, hdil=1)
+    args.update(bad)
+    s = cglib.Shape(*[args[k] for k in ("b", "h", "w", "c", "kn", "kh", "kw", "vpad", "hpad", "vstride",
+                                        "hstride", "vdil", "hdil")])
+    L = cglib.lib()
+    st = L.convgemm_fwd_f32(0, ctypes.byref(s), 1, 1, 1, None, None)   # non-NULL dummies: never dereferenced
+    assert st == 1, cglib.last_error()
+    assert cglib.last_error()[0] == 1
+    assert L.convgemm_wgrad_f32_workspace_size(ctypes.byref(s)) == 0
+
+
+def test_dropin_records_error_instead_of_crashing(cglib):
+    """The void drop-in reports bad geometry through the last-error API."""
+    with pytest.raises(cglib.ConvGemmError) as ei:
+        cglib.sconvGemmNHWC("N", 1, 2, 2, 3, 4, 5, 5, 0, 0, 1, 1, 1, 1, None, None, None)
+    assert ei.value.status == 1
+
+
+def test_batchnorm_needs_all_parameters(cglib):
+    s = cglib.Shape.of(1, 5, 5, 3, 4, 3, 3)
+    e = cglib.Epilogue(None, 1, None, None, None, 0)
+    st = cglib.lib().convgemm_fwd_f32(0, ctypes.byref(s), 1, 1, 1, ctypes.byref(e), None)
+    assert st == 1 and "batch-norm" in cglib.last_error()[1]
+
+
+def test_workspace_size_query(cglib):
+    s = cglib.Shape.of(2, 10, 10, 4, 8, 3, 3, 1, 1)
+    n = cglib.wgrad_f32_workspace_size(s)
+    nblocks = -(-(2 * 10 * 10) // 384)
+    assert n == 4 * nblocks * 36 * 8

@@ -1,0 +1,171 @@
+"""GPU parity of the FP32 plain form (the drop-in) against the reference.
+
+Each case runs through the reference-facing C ABI (sconvGemm* with host
+pointers, as a C caller of the reference would, and with device pointers) and
+through the extended API, and is compared with
+  * the reference's own outputs (golden fixtures): normwise and element-wise
+    relative error <= 1e-5 (tests/parity.py);
+  * the FP32 restatement of the reference's summation order (oracle, built on
+    this host): bit for bit for the forward pass and the weight gradient;
+  * the FP64 direct convolution at larger sizes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases as C
+from parity import FP32_TOL, bitexact, errors
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+torch = pytest.importorskip("torch")
+
+
+def gold(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))["out"]
+
+
+def dropin(cg, op, layout, g, inp, out, to_dev=False):
+    """Calls the reference-named entry point exactly as the reference's callers do."""
+    conv = cg.sconvGemmNHWC if layout == C.NHWC else cg.sconvGemmNCHW
+    back = cg.sconvGemmNHWC_back if layout == C.NHWC else cg.sconvGemmNCHW_back
+    dims = (g["b"], g["h"], g["w"], g["c"]) if layout == C.NHWC else (g["b"], g["c"], g["h"], g["w"])
+    cv = (lambda a: None if a is None else torch.from_numpy(a).cuda()) if to_dev else (lambda a: a)
+    e = inp["epi"]
+    if to_dev:
+        out_t = torch.from_numpy(out).cuda()
+    else:
+        out_t = out
+    if op == "fwd":
+        conv("N", *dims, g["kn"], g["kh"], g["kw"], g["vpad"], g["hpad"], g["vstr"], g["hstr"], g["vdil"], g["hdil"],
+             cv(inp["w"]), cv(inp["x"]), out_t, cv(e.get("bias")), cv(e.get("mean")), cv(e.get("inv_std")),
+             cv(e.get("gamma")), cv(e.get("beta")), e.get("relu", False))
+    elif op == "wgrad":
+        conv("T", *dims, g["kn"], g["kh"], g["kw"], g["vpad"], g["hpad"], g["vstr"], g["hstr"], g["vdil"], g["hdil"],
+             cv(inp["dy"]), cv(inp["x"]), out_t)
+    else:
+        back(*dims, g["kn"], g["kh"], g["kw"], g["vstr"], g["hstr"], g["vpad"], g["hpad"], g["vdil"], g["hdil"],
+             cv(inp["w"]), cv(inp["dy"]), out_t)
+    if to_dev:
+        torch.cuda.synchronize()
+        return out_t.cpu().numpy()
+    return out_t
+
+
+def port(O, op, layout, g, inp, n):
+    if op == "fwd":
+        return O.call_fwd("port", layout, g, inp["w"], inp["x"], np.zeros(n, np.float32), inp["epi"])
+    if op == "wgrad":
+        return O.call_fwd("port", layout, g, inp["dy"], inp["x"], np.zeros(n, np.float32), None, trans="T")
+    return O.call_back("port", layout, g, inp["w"], inp["dy"], inp["dx0"].copy())
+
+
+@pytest.mark.parametrize("case", C.CASES, ids=[c[0] for c in C.CASES])
+def test_dropin_matches_reference(cglib, oracle_lib, case):
+    name, op, layout, g, epi_kind, data = case
+    inp = C.make_inputs(*case)
+    ref = gold(name)
+    out0 = inp["dx0"].copy() if op == "dgrad" else np.full(ref.size, np.nan, np.float32)
+    host = dropin(cglib, op, layout, g, inp, out0.copy(), to_dev=False)
+    nw, ew = errors(host, ref)
+    assert nw <= FP32_TOL and ew <= FP32_TOL, (nw, ew)
+    dev = dropin(cglib, op, layout, g, inp, out0.copy(), to_dev=True)
+    assert bitexact(host, dev), "host-staged and device-pointer calls must agree"
+    if op != "dgrad":
+        assert bitexact(host, port(oracle_lib, op, layout, g, inp, ref.size)), \
+            "forward / weight gradient must follow the reference's summation order exactly"
+
+
+def test_config1_bitexact_with_reference(cglib):
+    """Config 1 (NHWC fwd, b=8 28x28 64->64 3x3 bias+ReLU): identical bits to the reference's output."""
+    case = C.CASES[0]
+    inp = C.make_inputs(*case)
+    ref = gold(case[0])
+    out = dropin(cglib, "fwd", C.NHWC, case[3], inp, np.zeros(ref.size, np.float32))
+    assert bitexact(out, ref)
+
+
+def _rand_geom(rng):
+    while True:
+        g = C.geom(int(rng.integers(1, 4)), int(rng.integers(3, 20)), int(rng.integers(3, 20)),
+                   int(rng.integers(1, 70)), int(rng.integers(1, 150)), int(rng.choice([1, 2, 3, 5])),
+                   int(rng.choice([1, 3, 4])), vpad=int(rng.integers(0, 3)), hpad=int(rng.integers(0, 3)),
+                   vstr=int(rng.integers(1, 4)), hstr=int(rng.integers(1, 3)), vdil=int(rng.integers(1, 3)),
+                   hdil=int(rng.integers(1, 3)))
+        ho, wo = C.out_hw(g)
+        if ho >= 1 and wo >= 1:
+            return g
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_shapes_against_restatement(cglib, oracle_lib, seed):
+    """Ragged sizes (partial tiles in every dimension, odd strides/dilations/paddings)."""
+    rng = np.random.default_rng(100 + seed)
+    g = _rand_geom(rng)
+    ho, wo = C.out_hw(g)
+    K = g["c"] * g["kh"] * g["kw"]
+    for layout in (C.NHWC, C.NCHW):
+        inp = {"x": rng.uniform(-1, 1, g["b"] * g["h"] * g["w"] * g["c"]).astype(np.float32),
+               "w": rng.standard_normal(K * g["kn"]).astype(np.float32),
+               "dy": rng.uniform(-1, 1, g["b"] * ho * wo * g["kn"]).astype(np.float32),
+               "dx0": rng.uniform(-1, 1, g["b"] * g["h"] * g["w"] * g["c"]).astype(np.float32),
+               "epi": {"bias": rng.uniform(-.1, .1, g["kn"]).astype(np.float32), "relu": True}}
+        for op, n in (("fwd", g["b"] * ho * wo * g["kn"]), ("wgrad", K * g["kn"]), ("dgrad", None)):
+            out0 = inp["dx0"].copy() if op == "dgrad" else np.zeros(n, np.float32)
+            got = dropin(cglib, op, layout, g, inp, out0, to_dev=True)
+            want = port(oracle_lib, op, layout, g, inp, n)
+            if op == "dgrad":
+                nw, ew = errors(got, want)
+                assert nw <= FP32_TOL, (g, layout, nw)
+            else:
+                assert bitexact(got, want), (g, layout, op)
+
+
+def test_extended_api_streams_and_determinism(cglib):
+    """convgemm_*_f32 on a side stream; weight and input gradients are bit-reproducible."""
+    cg = cglib
+    g = C.geom(4, 28, 28, 64, 96, 3, 3, pad=1, stride=2)
+    s = cg.Shape.of(g["b"], g["h"], g["w"], g["c"], g["kn"], 3, 3, 1, 1, 2, 2, 1, 1)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand(g["b"], g["h"], g["w"], g["c"], device="cuda", generator=gen) * 2 - 1
+    w = torch.randn(g["c"] * 9, g["kn"], device="cuda", generator=gen)
+    dy = torch.randn(g["b"], s.ho, s.wo, g["kn"], device="cuda", generator=gen)
+    ws = torch.empty(cg.wgrad_f32_workspace_size(s) // 4, device="cuda")
+    st = torch.cuda.Stream()
+    outs = []
+    with torch.cuda.stream(st):
+        for _ in range(2):
+            dw = torch.empty(g["c"] * 9, g["kn"], device="cuda")
+            dx = torch.empty_like(x)
+            cg.wgrad_f32(cg.NHWC, s, dy, x, dw, ws, stream=st)
+            cg.dgrad_f32(cg.NHWC, s, w, dy, dx, accumulate=False, stream=st)
+            outs.append((dw.clone(), dx.clone()))
+    st.synchronize()
+    cg.check_device(st)
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+    # against torch's own FP64 convolution
+    xd = x.double().permute(0, 3, 1, 2)
+    wd = w.double().reshape(g["c"], 3, 3, g["kn"]).permute(3, 0, 1, 2)
+    dyd = dy.double().permute(0, 3, 1, 2)
+    dx_ref = torch.nn.grad.conv2d_input(xd.shape, wd, dyd, stride=2, padding=1)
+    dw_ref = torch.nn.grad.conv2d_weight(xd, wd.shape, dyd, stride=2, padding=1)
+    assert errors(outs[0][1].permute(0, 3, 1, 2).cpu().numpy(), dx_ref.cpu().numpy())[0] < FP32_TOL
+    assert errors(outs[0][0].reshape(g["c"], 3, 3, g["kn"]).permute(3, 0, 1, 2).cpu().numpy(),
+                  dw_ref.cpu().numpy())[0] < FP32_TOL
+
+
+def test_resnet_layer_against_fp64(cglib, oracle_lib):
+    """A ResNet-50 stage-2 3x3 layer at batch 4, checked on sampled outputs in FP64."""
+    cg = cglib
+    O = oracle_lib
+    g = C.geom(4, 56, 56, 64, 64, 3, 3, pad=1)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(4 * 56 * 56 * 64).astype(np.float32)
+    w = (rng.standard_normal(576 * 64) * np.sqrt(2 / 576)).astype(np.float32)
+    y = np.zeros(4 * 56 * 56 * 64, np.float32)
+    cg.sconvGemmNHWC("N", 4, 56, 56, 64, 64, 3, 3, 1, 1, 1, 1, 1, 1, w, x, y)
+    idx = rng.choice(y.size, 4000, replace=False)
+    want = O.fwd_points_f64(0, g, w, x, idx)
+    assert errors(y[idx], want)[0] < FP32_TOL
