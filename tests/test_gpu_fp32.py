@@ -3,8 +3,9 @@
 Each case runs through the reference-facing C ABI (sconvGemm* with host
 pointers, as a C caller of the reference would, and with device pointers) and
 through the extended API, and is compared with
-  * the reference's own outputs (golden fixtures): normwise and element-wise
-    relative error <= 1e-5 (tests/parity.py);
+  * the reference's own outputs (golden fixtures): normwise and componentwise
+    relative error <= 1e-5, and the reference's own element-wise ratio on its
+    all-positive data (tests/parity.py);
   * the FP32 restatement of the reference's summation order (oracle, built on
     this host): bit for bit for the forward pass and the weight gradient;
   * the FP64 direct convolution at larger sizes.
@@ -15,7 +16,7 @@ import numpy as np
 import pytest
 
 import cases as C
-from parity import FP32_TOL, bitexact, errors
+from parity import FP32_TOL, bitexact, componentwise, elementwise_ref_check, errors, magnitude
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -69,8 +70,10 @@ def test_dropin_matches_reference(cglib, oracle_lib, case):
     ref = gold(name)
     out0 = inp["dx0"].copy() if op == "dgrad" else np.full(ref.size, np.nan, np.float32)
     host = dropin(cglib, op, layout, g, inp, out0.copy(), to_dev=False)
-    nw, ew = errors(host, ref)
-    assert nw <= FP32_TOL and ew <= FP32_TOL, (nw, ew)
+    assert errors(host, ref)[0] <= FP32_TOL
+    assert componentwise(host, ref, magnitude(oracle_lib, op, layout, g, inp)) <= FP32_TOL
+    if data == "positive":
+        assert elementwise_ref_check(host, ref) <= FP32_TOL
     dev = dropin(cglib, op, layout, g, inp, out0.copy(), to_dev=True)
     assert bitexact(host, dev), "host-staged and device-pointer calls must agree"
     if op != "dgrad":
@@ -117,8 +120,8 @@ def test_random_shapes_against_restatement(cglib, oracle_lib, seed):
             got = dropin(cglib, op, layout, g, inp, out0, to_dev=True)
             want = port(oracle_lib, op, layout, g, inp, n)
             if op == "dgrad":
-                nw, ew = errors(got, want)
-                assert nw <= FP32_TOL, (g, layout, nw)
+                assert errors(got, want)[0] <= FP32_TOL, (g, layout)
+                assert componentwise(got, want, magnitude(oracle_lib, op, layout, g, inp)) <= FP32_TOL
             else:
                 assert bitexact(got, want), (g, layout, op)
 

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import cases as C
-from parity import FP32_TOL, bitexact, errors
+from parity import FP32_TOL, bitexact, componentwise, elementwise_ref_check, errors, magnitude
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -59,9 +59,13 @@ def test_oracle_against_reference_outputs(oracle_lib, case):
     f64 = f64_result(O, op, layout, g, inp)
     nw, ew = errors(ref, f64)
     assert nw < 2e-6, f"reference vs FP64 normwise {nw}"
+    mag = magnitude(O, op, layout, g, inp)
+    assert componentwise(ref, f64, mag) < 1e-6
     port = port_result(O, op, layout, g, inp, ref.size)
-    nw, ew = errors(port, ref)
-    assert nw <= FP32_TOL and ew <= FP32_TOL, (nw, ew)
+    assert errors(port, ref)[0] <= FP32_TOL
+    assert componentwise(port, ref, mag) <= FP32_TOL
+    if data == "positive":
+        assert elementwise_ref_check(port, ref) <= FP32_TOL
     if name in BITEXACT:
         assert bitexact(port, ref), "restatement must match the reference bit for bit"
 
@@ -74,16 +78,17 @@ def test_planted_mistake_is_caught(oracle_lib):
     inp = C.make_inputs(*case)
     ref = load(name)["out"]
     good = O.fwd_f64(layout, g, inp["w"], inp["x"], inp["epi"]).ravel()
-    assert max(errors(good, ref)) <= FP32_TOL
+    mag = magnitude(O, op, layout, g, inp)
+    assert errors(good, ref)[0] <= FP32_TOL and componentwise(good, ref, mag) <= FP32_TOL
     bad = good.copy()
     bad[np.argmax(np.abs(bad))] *= 1.0001
-    assert max(errors(bad, ref)) > FP32_TOL
+    assert errors(bad, ref)[0] > FP32_TOL and componentwise(bad, ref, mag) > FP32_TOL
     # a mistake in the index semantics (padding taken on the wrong side) is far out
     g2 = dict(g, vpad=g["vpad"] + 1, h=g["h"] + 1)
     x2 = np.zeros((g["b"], g["h"] + 1, g["w"], g["c"]), np.float32)
     x2[:, 1:] = inp["x"].reshape(g["b"], g["h"], g["w"], g["c"])
     wrong = O.fwd_f64(layout, dict(g2, vpad=g["vpad"]), inp["w"], x2.ravel(), inp["epi"]).ravel()[:ref.size]
-    assert max(errors(wrong, ref)) > 1e-2
+    assert errors(wrong, ref)[0] > 1e-2
 
 
 def test_explicit_im2row_matches_direct(oracle_lib):
