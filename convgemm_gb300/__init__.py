@@ -95,6 +95,13 @@ def lib():
         L.convgemm_wgrad_f32_workspace_size.restype = ctypes.c_size_t
         L.convgemm_wgrad_f32.argtypes = [_I, SP, _VP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
         L.convgemm_dgrad_f32.argtypes = [_I, SP, _VP, _VP, _VP, _I, _VP]
+        L.convgemm_bf16_weights_size.argtypes = [SP, _I]
+        L.convgemm_bf16_weights_size.restype = ctypes.c_size_t
+        L.convgemm_bf16_pack_weights.argtypes = [_I, SP, _I, _VP, _VP, _VP]
+        L.convgemm_fold_epilogue.argtypes = [_I, EP, _VP, _VP, _VP]
+        L.convgemm_to_bf16_nhwc.argtypes = [_I, _I, _I, _I, _I, _VP, _VP, _VP]
+        L.convgemm_fwd_bf16.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
+        L.convgemm_dgrad_bf16.argtypes = [SP, _VP, _VP, _VP, _VP]
         _lib = L
     return _lib
 

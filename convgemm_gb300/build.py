@@ -65,7 +65,7 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     if _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH_FLAGS, "-shared", "-o", LIB, *objs, "-lcuda"]
+        cmd = [nvcc(), *ARCH_FLAGS, "-shared", "-o", LIB, *objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

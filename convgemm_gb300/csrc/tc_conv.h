@@ -1,0 +1,41 @@
+// Parameters of the BF16 tensor-core implicit-GEMM convolution kernel.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "cg_common.cuh"
+
+constexpr int TC_MAXCLS = 16;   // stride-phase classes (input gradient, strides up to 4x4)
+constexpr int TC_MAXTAPS = 49;  // taps per class (7x7 filters)
+
+// One dense implicit GEMM: its rows are the output pixels (b, j, jw) of a grid
+// Hg x Wg, written to output pixel (oy0 + osy*j, ox0 + osx*jw); tap t reads the
+// input pixel (j*isy + iby + toy[t], jw*isx + ibx + tox[t]).
+struct TcClass {
+    int Hg, Wg;
+    int oy0, ox0, osy, osx;
+    int isy, isx, iby, ibx;
+    int ntaps;
+    int kbeg;    // first K column of this class in the packed weights (multiple of 64)
+    int ktiles;  // K / 64
+    int mtiles;  // ceil(B*Hg*Wg / 128)
+    FastDiv dwg, dhg;
+    int16_t toy[TC_MAXTAPS], tox[TC_MAXTAPS];
+};
+
+struct TcConvParams {
+    const __nv_bfloat16 *in;   // gathered activation, NHWC [B][Hin][Win][Cin]
+    __nv_bfloat16 *out;        // NHWC [B][Hout][Wout][Cout]
+    const float *scale;        // per output channel, or NULL
+    const float *shift;        // per output channel, or NULL
+    int relu;
+    int B, Hin, Win, Cin, Hout, Wout, Cout;
+    FastDiv dcin;
+    int *err;                  // device error word for timed-out waits
+    int ncls;
+    TcClass cls[TC_MAXCLS];
+};
+
+cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &map, int bn, int mtiles_max, int ntiles,
+                           cudaStream_t st);

@@ -1,0 +1,310 @@
+// Host side of the BF16 tensor-core forms: problem planning (tap tables,
+// stride-phase classes of the input gradient), packed-weight layouts, TMA
+// tensor maps, and the public convgemm_*_bf16 entry points.
+#include <cstring>
+#include <mutex>
+
+#include "../../include/convgemm_gpu.h"
+#include "cg_common.cuh"
+#include "prep.h"
+#include "tc_conv.h"
+#include "tc_host.h"
+
+namespace {
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn) p;
+    });
+    return fn;
+}
+
+int pick_bn(int cout) { return cout >= 256 ? 256 : (cout > 64 ? 128 : 64); }
+
+}  // namespace
+
+// 2-D row-major [rows][cols] tensor, box {64 (cols), box_rows}, 128-byte swizzle.
+convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
+                                 long long rows, long long cols, int box_cols, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    if (((uintptr_t) ptr & 15) || ((cols * elem_bytes) & 15))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA operand not 16-byte aligned");
+    cuuint64_t dims[2] = {(cuuint64_t) cols, (cuuint64_t) rows};
+    cuuint64_t strides[1] = {(cuuint64_t) cols * elem_bytes};
+    cuuint32_t box[2] = {(cuuint32_t) box_cols, (cuuint32_t) box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int) r);
+    return CONVGEMM_SUCCESS;
+}
+
+// ------------------------------------------------------------ planning
+bool tc_plan_fwd(const cg_shape &s, TcPlan &pl) {
+    const ConvGeom g = make_geom(s);
+    if (s.kh * s.kw > TC_MAXTAPS) return false;
+    pl.Cin = round_up(s.c, 8);
+    pl.Cout = s.kn;
+    pl.Hin = s.h;
+    pl.Win = s.w;
+    pl.Hout = g.ho;
+    pl.Wout = g.wo;
+    pl.ncls = 1;
+    TcClass &c = pl.cls[0];
+    memset(&c, 0, sizeof(c));
+    c.Hg = g.ho;
+    c.Wg = g.wo;
+    c.oy0 = c.ox0 = 0;
+    c.osy = c.osx = 1;
+    c.isy = s.vstride;
+    c.isx = s.hstride;
+    c.iby = -s.vpad;
+    c.ibx = -s.hpad;
+    c.ntaps = s.kh * s.kw;
+    for (int kx = 0; kx < s.kh; kx++)
+        for (int ky = 0; ky < s.kw; ky++) {
+            c.toy[kx * s.kw + ky] = (int16_t) (kx * s.vdil);
+            c.tox[kx * s.kw + ky] = (int16_t) (ky * s.hdil);
+            pl.kx[0][kx * s.kw + ky] = (int8_t) kx;
+            pl.ky[0][kx * s.kw + ky] = (int8_t) ky;
+        }
+    c.kbeg = 0;
+    c.ktiles = (c.ntaps * pl.Cin + 63) / 64;
+    c.mtiles = (int) ((g.P + 127) / 128);
+    c.dwg = FastDiv(c.Wg);
+    c.dhg = FastDiv(c.Hg);
+    pl.Ktot = c.ktiles * 64;
+    pl.mtiles_max = c.mtiles;
+    pl.has_empty_class = false;
+    pl.bn = pick_bn(pl.Cout);
+    return true;
+}
+
+bool tc_plan_dgrad(const cg_shape &s, TcPlan &pl) {
+    const ConvGeom g = make_geom(s);
+    const int sy = s.vstride, sx = s.hstride;
+    if (sy * sx > TC_MAXCLS || s.kh * s.kw > TC_MAXTAPS) return false;
+    pl.Cin = round_up(s.kn, 8);   // the gathered tensor is dY
+    pl.Cout = s.c;
+    pl.Hin = g.ho;
+    pl.Win = g.wo;
+    pl.Hout = s.h;
+    pl.Wout = s.w;
+    pl.ncls = 0;
+    pl.has_empty_class = false;
+    pl.mtiles_max = 0;
+    int kb = 0;
+    for (int cy = 0; cy < sy; cy++)
+        for (int cx = 0; cx < sx; cx++) {
+            const int Hg = s.h > cy ? (s.h - cy + sy - 1) / sy : 0;
+            const int Wg = s.w > cx ? (s.w - cx + sx - 1) / sx : 0;
+            if (Hg == 0 || Wg == 0) continue;
+            TcClass &c = pl.cls[pl.ncls];
+            memset(&c, 0, sizeof(c));
+            int nt = 0;
+            for (int kx = 0; kx < s.kh; kx++) {
+                const int ty = cy + s.vpad - kx * s.vdil;
+                if (((ty % sy) + sy) % sy) continue;
+                for (int ky = 0; ky < s.kw; ky++) {
+                    const int tx = cx + s.hpad - ky * s.hdil;
+                    if (((tx % sx) + sx) % sx) continue;
+                    c.toy[nt] = (int16_t) (ty / sy);
+                    c.tox[nt] = (int16_t) (tx / sx);
+                    pl.kx[pl.ncls][nt] = (int8_t) kx;
+                    pl.ky[pl.ncls][nt] = (int8_t) ky;
+                    nt++;
+                }
+            }
+            if (nt == 0) {
+                pl.has_empty_class = true;
+                continue;
+            }
+            c.Hg = Hg;
+            c.Wg = Wg;
+            c.oy0 = cy;
+            c.ox0 = cx;
+            c.osy = sy;
+            c.osx = sx;
+            c.isy = c.isx = 1;
+            c.iby = c.ibx = 0;
+            c.ntaps = nt;
+            c.kbeg = kb;
+            c.ktiles = (nt * pl.Cin + 63) / 64;
+            kb += c.ktiles * 64;
+            c.mtiles = (int) (((long long) s.b * Hg * Wg + 127) / 128);
+            c.dwg = FastDiv(Wg);
+            c.dhg = FastDiv(Hg);
+            if (c.mtiles > pl.mtiles_max) pl.mtiles_max = c.mtiles;
+            pl.ncls++;
+        }
+    pl.Ktot = kb;
+    pl.bn = pick_bn(pl.Cout);
+    return true;
+}
+
+PackDgradInfo tc_pack_info(const TcPlan &pl) {
+    PackDgradInfo info;
+    memset(&info, 0, sizeof(info));
+    info.ncls = pl.ncls;
+    info.Ktot = pl.Ktot;
+    for (int c = 0; c < pl.ncls; c++) {
+        info.kbeg[c] = pl.cls[c].kbeg;
+        info.ntaps[c] = pl.cls[c].ntaps;
+        memcpy(info.kx[c], pl.kx[c], TC_MAXTAPS);
+        memcpy(info.ky[c], pl.ky[c], TC_MAXTAPS);
+    }
+    return info;
+}
+
+convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
+                         const float *scale, const float *shift, int relu, cudaStream_t st) {
+    if (pl.ncls == 0) return CONVGEMM_SUCCESS;
+    CUtensorMap map;
+    if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wpacked, pl.Cout, pl.Ktot, 64,
+                                             pl.bn))
+        return e;
+    TcConvParams p;
+    memset(&p, 0, sizeof(p));
+    p.in = (const __nv_bfloat16 *) in;
+    p.out = (__nv_bfloat16 *) out;
+    p.scale = scale;
+    p.shift = shift;
+    p.relu = relu;
+    p.B = s.b;
+    p.Hin = pl.Hin;
+    p.Win = pl.Win;
+    p.Cin = pl.Cin;
+    p.Hout = pl.Hout;
+    p.Wout = pl.Wout;
+    p.Cout = pl.Cout;
+    p.dcin = FastDiv(pl.Cin);
+    p.err = cg_device_error_word();
+    if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
+    p.ncls = pl.ncls;
+    for (int c = 0; c < pl.ncls; c++) p.cls[c] = pl.cls[c];
+    const int ntiles = (pl.Cout + pl.bn - 1) / pl.bn;
+    return cg_cuda_check(tc_conv_launch(p, map, pl.bn, pl.mtiles_max, ntiles, st), "tensor-core conv launch");
+}
+
+// ------------------------------------------------------------ public API
+namespace {
+convgemm_status_t check_tc_shape(const convgemm_shape_t *shape, const char *fn) {
+    if (!shape) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: shape is NULL", fn);
+    const convgemm_shape_t &s = *shape;
+    if (s.b < 1 || s.h < 1 || s.w < 1 || s.c < 1 || s.kn < 1 || s.kh < 1 || s.kw < 1 || s.vstride < 1 ||
+        s.hstride < 1 || s.vdil < 1 || s.hdil < 1 || s.vpad < 0 || s.hpad < 0)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: invalid geometry", fn);
+    const long long ho = (s.h + 2LL * s.vpad - (long long) s.vdil * (s.kh - 1) - 1) / s.vstride + 1;
+    const long long wo = (s.w + 2LL * s.hpad - (long long) s.hdil * (s.kw - 1) - 1) / s.hstride + 1;
+    if (s.h + 2LL * s.vpad - (long long) s.vdil * (s.kh - 1) < 1 || s.w + 2LL * s.hpad - (long long) s.hdil * (s.kw - 1) < 1)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: the filter does not fit the padded input", fn);
+    const long long lim = (1LL << 31) - 1;
+    if ((long long) s.b * s.h * s.w * round_up(s.c, 8) > lim || (long long) s.b * ho * wo * round_up(s.kn, 8) > lim)
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: a tensor has more than 2^31-1 elements", fn);
+    if (s.kh * s.kw > TC_MAXTAPS)
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: filters above 49 taps have no tensor-core kernel", fn);
+    return CONVGEMM_SUCCESS;
+}
+}  // namespace
+
+extern "C" size_t convgemm_bf16_weights_size(const convgemm_shape_t *shape, int kind) {
+    if (check_tc_shape(shape, "convgemm_bf16_weights_size")) return 0;
+    const cg_shape s = cg_from_public(*shape);
+    TcPlan pl;
+    if (kind == CONVGEMM_OPERAND_FWD) {
+        if (!tc_plan_fwd(s, pl)) return 0;
+    } else if (kind == CONVGEMM_OPERAND_DGRAD) {
+        if (!tc_plan_dgrad(s, pl)) return 0;
+    } else {
+        return 0;
+    }
+    return (size_t) pl.Cout * (size_t) (pl.Ktot > 0 ? pl.Ktot : 64) * 2;
+}
+
+extern "C" convgemm_status_t convgemm_bf16_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                                        int kind, const float *weights, void *packed, void *stream) {
+    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_bf16_pack_weights")) return e;
+    if (!weights || !packed) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_bf16_pack_weights: NULL");
+    const cg_shape s = cg_from_public(*shape);
+    const int nchw = layout == CONVGEMM_NCHW;
+    TcPlan pl;
+    cudaStream_t st = (cudaStream_t) stream;
+    if (kind == CONVGEMM_OPERAND_FWD) {
+        tc_plan_fwd(s, pl);
+        return cg_cuda_check(prep_pack_fwd(weights, nchw, s.c, s.kh, s.kw, s.kn, pl.Cin, pl.Ktot, packed, st),
+                             "pack weights");
+    }
+    if (kind == CONVGEMM_OPERAND_DGRAD) {
+        if (!tc_plan_dgrad(s, pl))
+            return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "input gradient: more than 16 stride-phase classes");
+        if (pl.Ktot == 0) return CONVGEMM_SUCCESS;
+        return cg_cuda_check(prep_pack_dgrad(weights, nchw, s.c, s.kh, s.kw, s.kn, pl.Cin, tc_pack_info(pl), packed, st),
+                             "pack weights");
+    }
+    return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_bf16_pack_weights: bad kind %d", kind);
+}
+
+extern "C" convgemm_status_t convgemm_fold_epilogue(int kn, const convgemm_epilogue_t *epi, float *scale,
+                                                    float *shift, void *stream) {
+    if (kn < 1 || !scale || !shift) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_fold_epilogue: bad args");
+    convgemm_epilogue_t e = {};
+    if (epi) e = *epi;
+    if (e.mean && !(e.inv_std && e.gamma && e.beta))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_fold_epilogue: batch-norm needs all parameters");
+    return cg_cuda_check(prep_fold(kn, e.bias, e.mean, e.inv_std, e.gamma, e.beta, scale, shift, (cudaStream_t) stream),
+                         "fold epilogue");
+}
+
+extern "C" convgemm_status_t convgemm_to_bf16_nhwc(convgemm_layout_t layout, int b, int c, int h, int w,
+                                                   const float *in, void *out, void *stream) {
+    if (b < 1 || c < 1 || h < 1 || w < 1 || !in || !out)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_to_bf16_nhwc: bad args");
+    return cg_cuda_check(prep_to_bf16_nhwc(in, layout == CONVGEMM_NCHW, b, c, h, w, round_up(c, 8), out,
+                                           (cudaStream_t) stream),
+                         "cast to bf16");
+}
+
+extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, const void *x, const void *wpacked,
+                                               void *y, const float *scale, const float *shift, int relu,
+                                               void *stream) {
+    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_fwd_bf16")) return e;
+    if (!x || !wpacked || !y) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_fwd_bf16: NULL tensor");
+    if (shape->kn % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "convgemm_fwd_bf16: kn must be a multiple of 8");
+    const cg_shape s = cg_from_public(*shape);
+    TcPlan pl;
+    tc_plan_fwd(s, pl);
+    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream);
+}
+
+extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
+                                                 void *dx, void *stream) {
+    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_dgrad_bf16")) return e;
+    if (!dy || !wpacked || !dx) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16: NULL tensor");
+    if (shape->c % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "convgemm_dgrad_bf16: c must be a multiple of 8");
+    const cg_shape s = cg_from_public(*shape);
+    TcPlan pl;
+    if (!tc_plan_dgrad(s, pl))
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "input gradient: more than 16 stride-phase classes");
+    cudaStream_t st = (cudaStream_t) stream;
+    if (pl.has_empty_class) {
+        // pixels no tap reaches receive zero
+        if (convgemm_status_t e = cg_cuda_check(
+                cudaMemsetAsync(dx, 0, sizeof(__nv_bfloat16) * (size_t) s.b * s.h * s.w * s.c, st), "zero dx"))
+            return e;
+    }
+    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st);
+}

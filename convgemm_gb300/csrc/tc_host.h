@@ -1,0 +1,25 @@
+// Planning structures shared by the tensor-core host code.
+#pragma once
+#include <cuda.h>
+
+#include "../../include/convgemm_gpu.h"
+#include "cg_internal.h"
+#include "prep.h"
+#include "tc_conv.h"
+
+// A planned tensor-core convolution: its classes, and the packed-operand geometry.
+struct TcPlan {
+    int Cin, Cout, Hin, Win, Hout, Wout;
+    int ncls, Ktot, mtiles_max, bn;
+    bool has_empty_class;
+    TcClass cls[TC_MAXCLS];
+    int8_t kx[TC_MAXCLS][TC_MAXTAPS], ky[TC_MAXCLS][TC_MAXTAPS];
+};
+
+bool tc_plan_fwd(const cg_shape &s, TcPlan &pl);
+bool tc_plan_dgrad(const cg_shape &s, TcPlan &pl);
+PackDgradInfo tc_pack_info(const TcPlan &pl);
+convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
+                                 long long rows, long long cols, int box_cols, int box_rows);
+convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
+                         const float *scale, const float *shift, int relu, cudaStream_t st);

@@ -88,6 +88,43 @@ convgemm_status_t convgemm_dgrad_f32(convgemm_layout_t layout, const convgemm_sh
                                      const float *weights, const float *dy, float *dx,
                                      int accumulate, void *stream);
 
+/* -------------------------------------------- BF16 tensor-core form (NHWC) */
+
+/* Which packed operand convgemm_bf16_pack_weights produces. */
+#define CONVGEMM_OPERAND_FWD 0    /* forward:        [kn][taps * c8], c8 = c rounded up to 8 */
+#define CONVGEMM_OPERAND_DGRAD 1  /* input gradient: [c][classes x taps x kn8], flipped taps */
+
+/* Bytes of a packed BF16 weight operand (0 if the shape has no tensor-core kernel). */
+size_t convgemm_bf16_weights_size(const convgemm_shape_t *shape, int kind);
+
+/* Packs FP32 weights in the reference layout of `layout` (NHWC API: [c][kh][kw][kn];
+ * NCHW API: [kn][c][kh][kw]) into the BF16 operand of the tensor-core kernels. */
+convgemm_status_t convgemm_bf16_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape, int kind,
+                                             const float *weights, void *packed, void *stream);
+
+/* Folds bias and batch-norm into per-channel scale/shift in FP64 on the GPU:
+ * scale = gamma*inv_std, shift = beta + (bias - mean)*scale (identity without BN). */
+convgemm_status_t convgemm_fold_epilogue(int kn, const convgemm_epilogue_t *epi, float *scale, float *shift,
+                                         void *stream);
+
+/* FP32 activations (NHWC, or NCHW [b][c][h][w]) -> BF16 NHWC with the channel
+ * dimension padded to a multiple of 8 (padding zero), as the BF16 kernels read them. */
+convgemm_status_t convgemm_to_bf16_nhwc(convgemm_layout_t layout, int b, int c, int h, int w, const float *in,
+                                        void *out, void *stream);
+
+/* Forward, BF16 tensor cores (tcgen05, FP32 accumulation in TMEM): generalises
+ * sconvGemmNHWC('N') (src/convGemm.c:65-70).  x: BF16 NHWC [b][h][w][c8];
+ * y: BF16 NHWC [b][ho][wo][kn] = relu?(acc*scale + shift); scale/shift may be NULL.
+ * Needs kn % 8 == 0. */
+convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, const void *x, const void *wpacked, void *y,
+                                    const float *scale, const float *shift, int relu, void *stream);
+
+/* Input gradient, BF16 tensor cores, gather form (no col2im scatter):
+ * generalises sconvGemmNHWC_back (src/convGemm.c:82-97).  dy: BF16 NHWC
+ * [b][ho][wo][kn8]; dx: BF16 NHWC [b][h][w][c], overwritten.  Needs c % 8 == 0. */
+convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
+                                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif

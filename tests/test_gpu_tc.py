@@ -1,0 +1,125 @@
+"""GPU tests of the BF16 tensor-core form (tcgen05 + TMEM + TMA).
+
+Each result is compared with the FP64 direct-convolution oracle run on the
+same BF16-rounded inputs (so the only differences left are FP32 accumulation
+and the BF16 rounding of the output) and with the FP64 result of the original
+FP32 inputs, where the stated target is max relative error <= 1e-2.
+"""
+import numpy as np
+import pytest
+
+import cases as C
+from parity import rel_max_rms
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+BF16_TOL = 1e-2        # stated target vs FP64 of the FP32 inputs (normwise max relative error)
+BF16_SELF_TOL = 6e-3   # vs FP64 of the BF16-rounded inputs: output rounding (2^-9) + FP32 accumulation
+
+
+def bf16r(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(torch.bfloat16).float().numpy()
+
+
+def to_dev_bf16_nhwc(cg, tc, x_nhwc, b, c, h, w):
+    xt = torch.from_numpy(x_nhwc).cuda()
+    out = torch.empty(b, h, w, tc.c8(c), dtype=torch.bfloat16, device="cuda")
+    tc.to_bf16_nhwc(cg.NHWC, b, c, h, w, xt, out)
+    return out
+
+
+def pack(cg, tc, s, kind, w):
+    nbytes = tc.weights_size(s, kind)
+    assert nbytes > 0
+    packed = torch.empty(nbytes // 2, dtype=torch.bfloat16, device="cuda")
+    tc.pack_weights(cg.NHWC, s, kind, torch.from_numpy(w).cuda(), packed)
+    return packed
+
+
+FWD_SHAPES = [
+    # b, h, w, c, kn, k, pad, stride, dil
+    (2, 14, 14, 64, 64, 3, 1, 1, 1),
+    (2, 14, 14, 64, 256, 1, 0, 1, 1),
+    (2, 9, 9, 128, 128, 3, 1, 2, 1),
+    (3, 7, 7, 512, 512, 3, 1, 1, 1),
+    (2, 20, 20, 3, 64, 7, 3, 2, 1),      # stem-like: 3 channels padded to 8
+    (1, 13, 11, 40, 72, 3, 2, 1, 2),     # ragged channels, dilation
+    (2, 8, 8, 256, 1024, 1, 0, 1, 1),
+    (1, 15, 15, 96, 192, 3, 1, 2, 1),
+]
+
+
+@pytest.mark.parametrize("shape", FWD_SHAPES, ids=[str(s) for s in FWD_SHAPES])
+def test_fwd_bf16_against_fp64(cglib, oracle_lib, shape):
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, stride=stride, dil=dil)
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(sum(shape))
+    K = c * k * k
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    wt = (rng.standard_normal(K * kn) * np.sqrt(2.0 / K)).astype(np.float32)
+    epi = {"bias": rng.uniform(-.1, .1, kn).astype(np.float32), "mean": rng.normal(0, .1, kn).astype(np.float32),
+           "inv_std": (1 / np.sqrt(rng.uniform(.5, 2, kn) + 1e-5)).astype(np.float32),
+           "gamma": rng.uniform(.5, 1.5, kn).astype(np.float32), "beta": rng.uniform(-.1, .1, kn).astype(np.float32),
+           "relu": True}
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
+    scale = torch.empty(kn, device="cuda")
+    shift = torch.empty(kn, device="cuda")
+    dev = {k_: torch.from_numpy(v).cuda() for k_, v in epi.items() if k_ != "relu"}
+    tc.fold_epilogue(kn, scale, shift, **dev)
+    y = torch.empty(b, s.ho, s.wo, kn, dtype=torch.bfloat16, device="cuda")
+    tc.fwd_bf16(s, xd, wp, y, scale, shift, relu=True)
+    torch.cuda.synchronize()
+    cg.check_device()
+    got = y.float().cpu().numpy().ravel()
+    ref_r = O.fwd_f64(C.NHWC, g, bf16r(wt), bf16r(x), epi).ravel()
+    ref = O.fwd_f64(C.NHWC, g, wt, x, epi).ravel()
+    e_self, _ = rel_max_rms(got, ref_r)
+    e_max, e_rms = rel_max_rms(got, ref)
+    assert e_self <= BF16_SELF_TOL, e_self
+    assert e_max <= BF16_TOL, (e_max, e_rms)
+    # deterministic
+    y2 = torch.empty_like(y)
+    tc.fwd_bf16(s, xd, wp, y2, scale, shift, relu=True)
+    torch.cuda.synchronize()
+    assert torch.equal(y.view(torch.int16), y2.view(torch.int16))
+
+
+DGRAD_SHAPES = [
+    (2, 14, 14, 64, 64, 3, 1, 1, 1),
+    (2, 14, 14, 64, 128, 3, 1, 2, 1),    # four stride-phase classes
+    (2, 14, 14, 256, 512, 1, 0, 2, 1),   # 1x1/s2: three classes receive no tap -> zeros
+    (2, 13, 13, 64, 64, 7, 3, 2, 1),
+    (1, 12, 10, 32, 48, 3, 2, 1, 2),
+    (3, 7, 7, 512, 512, 3, 1, 1, 1),
+    (2, 9, 9, 128, 64, 3, 0, 2, 1),      # no padding, odd size
+]
+
+
+@pytest.mark.parametrize("shape", DGRAD_SHAPES, ids=[str(s) for s in DGRAD_SHAPES])
+def test_dgrad_bf16_against_fp64(cglib, oracle_lib, shape):
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, stride=stride, dil=dil)
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(7 + sum(shape))
+    K = c * k * k
+    wt = (rng.standard_normal(K * kn) * np.sqrt(2.0 / K)).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    wp = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    dx = torch.full((b, h, w, c), float("nan"), dtype=torch.bfloat16, device="cuda")
+    tc.dgrad_bf16(s, dyd, wp, dx)
+    torch.cuda.synchronize()
+    cg.check_device()
+    got = dx.float().cpu().numpy().ravel()
+    assert np.isfinite(got).all(), "every input-gradient pixel must be written"
+    ref_r = O.dgrad_f64(C.NHWC, g, bf16r(wt), bf16r(dy))
+    ref = O.dgrad_f64(C.NHWC, g, wt, dy)
+    assert rel_max_rms(got, ref_r)[0] <= BF16_SELF_TOL
+    assert rel_max_rms(got, ref)[0] <= BF16_TOL
