@@ -102,6 +102,9 @@ def lib():
         L.convgemm_to_bf16_nhwc.argtypes = [_I, _I, _I, _I, _I, _VP, _VP, _VP]
         L.convgemm_fwd_bf16.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_dgrad_bf16.argtypes = [SP, _VP, _VP, _VP, _VP]
+        L.convgemm_wgrad_bf16_workspace_size.argtypes = [SP]
+        L.convgemm_wgrad_bf16_workspace_size.restype = ctypes.c_size_t
+        L.convgemm_wgrad_bf16.argtypes = [_I, SP, _VP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
         _lib = L
     return _lib
 

@@ -308,3 +308,104 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, 
     }
     return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st);
 }
+
+// ------------------------------------------------------- weight gradient
+#include "tc_wgrad.h"
+
+namespace {
+
+struct WgPlan {
+    int xa, bn, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
+    size_t ws_bytes;
+};
+
+WgPlan plan_wgrad(const cg_shape &s) {
+    const ConvGeom g = make_geom(s);
+    WgPlan w;
+    w.Cp = round_up(s.c, 8);
+    w.kn8 = round_up(s.kn, 8);
+    w.Nx = s.kh * s.kw * w.Cp;
+    w.xa = s.kn < 128;
+    int Mext, Next;
+    if (w.xa) {
+        Mext = w.Nx;
+        Next = s.kn;
+        w.bn = s.kn <= 64 ? 64 : 128;
+    } else {
+        Mext = s.kn;
+        Next = w.Nx;
+        w.bn = w.Nx >= 256 ? 256 : (w.Nx > 64 ? 128 : 64);
+    }
+    w.mtiles = (Mext + 127) / 128;
+    w.ntiles = (Next + w.bn - 1) / w.bn;
+    w.nchunks = (int) ((g.P + 63) / 64);
+    const int base = w.mtiles * w.ntiles;
+    const int per_sm = w.bn == 256 ? 1 : 2;
+    int splits = (152 * per_sm + base - 1) / base;
+    const int max_splits = (w.nchunks + 7) / 8;  // at least 8 chunks (512 pixels) per split
+    if (splits > max_splits) splits = max_splits;
+    if (splits < 1) splits = 1;
+    w.cps = (w.nchunks + splits - 1) / splits;
+    w.splits = (w.nchunks + w.cps - 1) / w.cps;
+    w.ws_bytes = sizeof(float) * (size_t) w.splits * (size_t) w.Nx * (size_t) s.kn;
+    return w;
+}
+
+}  // namespace
+
+extern "C" size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape) {
+    if (check_tc_shape(shape, "convgemm_wgrad_bf16_workspace_size")) return 0;
+    return plan_wgrad(cg_from_public(*shape)).ws_bytes;
+}
+
+extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                                 const void *dy, const void *x, float *dw, void *workspace,
+                                                 size_t workspace_bytes, void *stream) {
+    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_wgrad_bf16")) return e;
+    if (!dy || !x || !dw || !workspace)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_wgrad_bf16: NULL tensor or workspace");
+    if (layout != CONVGEMM_NHWC && layout != CONVGEMM_NCHW)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_wgrad_bf16: bad layout %d", (int) layout);
+    const cg_shape s = cg_from_public(*shape);
+    const ConvGeom g = make_geom(s);
+    const WgPlan w = plan_wgrad(s);
+    if (workspace_bytes < w.ws_bytes)
+        return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "convgemm_wgrad_bf16: workspace %zu bytes < %zu needed",
+                            workspace_bytes, w.ws_bytes);
+    CUtensorMap map;
+    if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, w.kn8, 64, 64))
+        return e;
+    TcWgradParams p;
+    memset(&p, 0, sizeof(p));
+    p.x = (const __nv_bfloat16 *) x;
+    p.ws = (float *) workspace;
+    p.B = s.b;
+    p.H = s.h;
+    p.W = s.w;
+    p.Cp = w.Cp;
+    p.kh = s.kh;
+    p.kw = s.kw;
+    p.kn = s.kn;
+    p.Nx = w.Nx;
+    p.P = (int) g.P;
+    p.vstr = s.vstride;
+    p.hstr = s.hstride;
+    p.vpad = s.vpad;
+    p.hpad = s.hpad;
+    p.vdil = s.vdil;
+    p.hdil = s.hdil;
+    p.nchunks = w.nchunks;
+    p.chunks_per_split = w.cps;
+    p.dcp = FastDiv(w.Cp);
+    p.dwo = FastDiv(g.wo);
+    p.dho = FastDiv(g.ho);
+    p.err = cg_device_error_word();
+    if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
+    cudaStream_t st = (cudaStream_t) stream;
+    if (convgemm_status_t e = cg_cuda_check(
+            tc_wgrad_launch(p, map, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
+        return e;
+    return cg_cuda_check(tc_wgrad_reduce((const float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
+                                         s.kw, layout == CONVGEMM_NCHW, st),
+                         "weight-gradient reduction");
+}

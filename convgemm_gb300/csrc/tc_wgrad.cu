@@ -1,0 +1,275 @@
+// BF16 tensor-core weight gradient (sm_103a): the transposed GEMM of
+// sconvGemmNHWC('T') (src/convGemm.c:71-76),
+//     dW[co][n] = sum_p dY[p][co] * X_im2row[p][n],  n = tap*Cp + ci,
+// whose reduction runs over all b*ho*wo output pixels.  The pixels are cut
+// into 64-pixel chunks and the chunks into `splits` contiguous ranges, one per
+// blockIdx.z; each CTA writes its FP32 partial tile to a workspace and
+// wgrad_reduce adds the splits in increasing order, so the result is
+// bit-reproducible run to run (no float atomics).
+//
+// Both operands reach the tensor core MN-major (the pixel index is the slow,
+// K dimension in memory):
+//   dY side: TMA boxes of 64 channels x 64 pixels from dY viewed as [P][kn8];
+//   X side:  16-byte cp.async gathers of 8 channels of one tap for each pixel,
+//            zero-filled for padding, written in the 128-byte-swizzled layout.
+// The X side is the 128-row A operand when kn < 128 (template XA), else dY is,
+// so narrow layers do not waste half of each MMA.
+#include <cuda_bf16.h>
+
+#include "cg_common.cuh"
+#include "tc_ptx.cuh"
+#include "tc_wgrad.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+template <int BN, int STAGES, bool XA>
+struct WgCfg {
+    static constexpr int BM = 128, BK = 64;  // BK pixels per stage
+    static constexpr uint32_t A_BYTES = BM * BK * 2;
+    static constexpr uint32_t B_BYTES = BN * BK * 2;
+    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr int X_ATOMS = (XA ? BM : BN) / 64;    // 64-channel atoms gathered from X
+    static constexpr int DY_ATOMS = (XA ? BN : BM) / 64;   // 64-channel atoms loaded from dY
+    static constexpr uint32_t DY_BYTES = DY_ATOMS * 64 * BK * 2;
+    static constexpr int LAG = STAGES - 1;
+    static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
+};
+
+template <int BN, int STAGES, bool XA>
+__global__ void __launch_bounds__(160, 1)
+    tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap) {
+    using C = WgCfg<BN, STAGES, XA>;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
+    uint64_t *full = (uint64_t *) (base + STAGES * C::STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *accum = empty + STAGES;
+    uint32_t *tmem_holder = (uint32_t *) (accum + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            tc::mbar_init(&full[s], 128 + 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        tc::mbar_init(accum, 1);
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&dymap);
+    }
+    if (warp == 4) {
+        tc::tmem_alloc(tmem_holder, BN);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    // tile origins along the X extent (n = tap*Cp + ci) and the channel extent (co)
+    const int mrow0 = blockIdx.x * C::BM, ncol0 = blockIdx.y * BN;
+    const int x0 = XA ? mrow0 : ncol0;
+    const int co0 = XA ? ncol0 : mrow0;
+    const int chunk0 = blockIdx.z * p.chunks_per_split;
+    const int KT = min(p.chunks_per_split, p.nchunks - chunk0);
+    bool ok = true;
+
+    if (warp < 4) {
+        const int t = threadIdx.x;
+        const int piece = t & 7;
+        const int r0 = t >> 3;  // pixel rows r0 + 16*i, i < 4
+        // per X atom: the tap and channel of this thread's 8-channel piece (fixed for the CTA)
+        int a_ci[C::X_ATOMS], a_oy[C::X_ATOMS], a_ox[C::X_ATOMS];
+        bool a_ok[C::X_ATOMS];
+#pragma unroll
+        for (int a = 0; a < C::X_ATOMS; a++) {
+            const int n = x0 + 64 * a + 8 * piece;
+            uint32_t tap, ci;
+            p.dcp.divmod(n, tap, ci);
+            a_ok[a] = n < p.Nx;
+            const int kx = (int) tap / p.kw, ky = (int) tap % p.kw;
+            a_ci[a] = ci;
+            a_oy[a] = kx * p.vdil - p.vpad;
+            a_ox[a] = ky * p.hdil - p.hpad;
+        }
+        const uint32_t xoff = XA ? 0 : C::A_BYTES;  // X tile inside the stage
+        const uint32_t dyoff = XA ? C::A_BYTES : 0;
+        for (int kt = 0; kt < KT; kt++) {
+            const int s = kt % STAGES;
+            const uint32_t ph = (kt / STAGES) & 1;
+            if (kt >= STAGES) ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11);
+            if (!ok) break;
+            const int pbase = (chunk0 + kt) * C::BK;
+            const uint32_t sX = tc::smem_u32(base + s * C::STAGE_BYTES + xoff);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + 16 * i;
+                const int pix = pbase + r;
+                int bb = -1, iy0 = 0, ix0 = 0;
+                if (pix < p.P) {
+                    uint32_t q, ow, oh, b;
+                    p.dwo.divmod(pix, q, ow);
+                    p.dho.divmod(q, b, oh);
+                    bb = b;
+                    iy0 = (int) oh * p.vstr;
+                    ix0 = (int) ow * p.hstr;
+                }
+#pragma unroll
+                for (int a = 0; a < C::X_ATOMS; a++) {
+                    const int iy = iy0 + a_oy[a], ix = ix0 + a_ox[a];
+                    const bool v = bb >= 0 && a_ok[a] && (unsigned) iy < (unsigned) p.H && (unsigned) ix < (unsigned) p.W;
+                    const bf16 *src = v ? p.x + ((((size_t) bb * p.H + iy) * p.W + ix) * p.Cp + a_ci[a]) : p.x;
+                    tc::cp_async_16(sX + a * 8192 + r * 128 + ((piece ^ (r & 7)) << 4), src, v ? 16u : 0u);
+                }
+            }
+            tc::cp_async_commit();
+            if (t == 0) {
+                tc::mbar_arrive_expect_tx(&full[s], C::DY_BYTES);
+                const uint32_t sD = tc::smem_u32(base + s * C::STAGE_BYTES + dyoff);
+#pragma unroll
+                for (int a = 0; a < C::DY_ATOMS; a++) tc::tma_load_2d(sD + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
+            }
+            if (kt >= C::LAG) {
+                tc::cp_async_wait<C::LAG>();
+                tc::fence_proxy_async_smem();
+                tc::mbar_arrive(&full[(kt - C::LAG) % STAGES]);
+            }
+        }
+        tc::cp_async_wait<0>();
+        tc::fence_proxy_async_smem();
+        if (ok)
+            for (int kt = (KT > C::LAG ? KT - C::LAG : 0); kt < KT; kt++) tc::mbar_arrive(&full[kt % STAGES]);
+
+        // epilogue: FP32 partial tile -> workspace [split][Mext][Next]
+        if (ok) ok = tc::mbar_wait(accum, 0, p.err, 13);
+        tc::tc_fence_after();
+        const int m = mrow0 + warp * 32 + lane;
+        const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx;
+        float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
+        if (ok) {
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t v[32];
+                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+                tc::tmem_ld_wait();
+                const int nb = ncol0 + c0;
+                if (m < Mext && nb < Next) {
+                    if (nb + 32 <= Next && (Next & 3) == 0) {
+                        float4 *dst = reinterpret_cast<float4 *>(wrow + nb);
+#pragma unroll
+                        for (int q = 0; q < 8; q++)
+                            dst[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
+                                                 __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
+                    } else {
+#pragma unroll
+                        for (int jj = 0; jj < 32; jj++)
+                            if (nb + jj < Next) wrow[nb + jj] = __uint_as_float(v[jj]);
+                    }
+                }
+            }
+        }
+    } else {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
+            for (int kt = 0; kt < KT; kt++) {
+                const int s = kt % STAGES;
+                const uint32_t ph = (kt / STAGES) & 1;
+                if (!tc::mbar_wait(&full[s], ph, p.err, 12)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
+                const uint32_t b0 = a0 + C::A_BYTES;
+#pragma unroll
+                for (int k = 0; k < C::BK / 16; k++) {
+                    const uint64_t ad = tc::sw128_desc(a0 + k * 2048, 8192, 1024);
+                    const uint64_t bd = tc::sw128_desc(b0 + k * 2048, 8192, 1024);
+                    tc::mma_f16(tmem, ad, bd, idesc, (kt | k) != 0);
+                }
+                tc::mma_commit(&empty[s]);
+            }
+            tc::mma_commit(accum);
+        }
+        __syncwarp();
+    }
+
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 4) tc::tmem_dealloc(tmem, BN);
+}
+
+// dW = sum over splits in increasing order, written in the requested layout:
+//   layout 0 (NHWC API): [ci][kh][kw][co];  layout 1 (NCHW API): [co][ci][kh][kw].
+__global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restrict__ dw, int splits, int xa, int Nx,
+                                    int kn, int C, int Cp, int kh, int kw, int layout) {
+    const long long total = (long long) C * kh * kw * kn;
+    const long long plane = (long long) Nx * kn;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x) {
+        int co, ci, kx, ky;
+        if (layout == 0) {
+            co = (int) (i % kn);
+            long long k = i / kn;
+            ky = (int) (k % kw);
+            kx = (int) ((k / kw) % kh);
+            ci = (int) (k / ((long long) kw * kh));
+        } else {
+            long long k = i % ((long long) C * kh * kw);
+            co = (int) (i / ((long long) C * kh * kw));
+            ky = (int) (k % kw);
+            kx = (int) ((k / kw) % kh);
+            ci = (int) (k / ((long long) kw * kh));
+        }
+        const long long n = (long long) (kx * kw + ky) * Cp + ci;
+        const long long off = xa ? n * kn + co : (long long) co * Nx + n;
+        float s = ws[off];
+        for (int z = 1; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
+        dw[i] = s;
+    }
+}
+
+template <int BN, int STAGES, bool XA>
+cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, dim3 grid, cudaStream_t st) {
+    using C = WgCfg<BN, STAGES, XA>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    kern<<<grid, 160, C::SMEM, st>>>(p, map);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, int bn, int xa, int mtiles, int ntiles,
+                            int splits, cudaStream_t st) {
+    dim3 grid(mtiles, ntiles, splits);
+    if (xa) {
+        switch (bn) {
+            case 64: return launch_wg<64, 4, true>(p, dymap, grid, st);
+            case 128: return launch_wg<128, 3, true>(p, dymap, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (bn) {
+        case 64: return launch_wg<64, 4, false>(p, dymap, grid, st);
+        case 128: return launch_wg<128, 3, false>(p, dymap, grid, st);
+        case 256: return launch_wg<256, 4, false>(p, dymap, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
+                            int kw, int layout, cudaStream_t st) {
+    const long long total = (long long) C * kh * kw * kn;
+    long long g = (total + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    wgrad_reduce_kernel<<<(int) g, 256, 0, st>>>(ws, dw, splits, xa, Nx, kn, C, Cp, kh, kw, layout);
+    return cudaGetLastError();
+}

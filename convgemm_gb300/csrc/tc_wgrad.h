@@ -1,0 +1,21 @@
+// Parameters of the BF16 tensor-core weight-gradient kernel.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "cg_common.cuh"
+
+struct TcWgradParams {
+    const __nv_bfloat16 *x;   // NHWC [B][H][W][Cp]
+    float *ws;                // [splits][Mext][Next] FP32 partial tiles
+    int B, H, W, Cp, kh, kw, kn, Nx, P;
+    int vstr, hstr, vpad, hpad, vdil, hdil;
+    int nchunks, chunks_per_split;  // 64-pixel chunks of the reduction, per split
+    FastDiv dcp, dwo, dho;
+    int *err;
+};
+
+cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, int bn, int xa, int mtiles, int ntiles,
+                            int splits, cudaStream_t st);
+cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
+                            int kw, int layout, cudaStream_t st);

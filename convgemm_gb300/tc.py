@@ -42,3 +42,13 @@ def fwd_bf16(shape: Shape, x, wpacked, y, scale=None, shift=None, relu=False, st
 
 def dgrad_bf16(shape: Shape, dy, wpacked, dx, stream=None):
     _raise_if(lib().convgemm_dgrad_bf16(ctypes.byref(shape), ptr(dy), ptr(wpacked), ptr(dx), _stream(stream)))
+
+
+def wgrad_bf16_workspace_size(shape: Shape) -> int:
+    return lib().convgemm_wgrad_bf16_workspace_size(ctypes.byref(shape))
+
+
+def wgrad_bf16(layout, shape: Shape, dy, x, dw, workspace, stream=None):
+    nbytes = workspace.numel() * workspace.element_size()
+    _raise_if(lib().convgemm_wgrad_bf16(layout, ctypes.byref(shape), ptr(dy), ptr(x), ptr(dw), ptr(workspace),
+                                        nbytes, _stream(stream)))

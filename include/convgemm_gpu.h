@@ -125,6 +125,18 @@ convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, const void *x
 convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
                                       void *stream);
 
+/* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
+size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);
+
+/* Weight gradient, BF16 tensor cores, split over pixels with a fixed-order
+ * reduction (bit-reproducible): generalises sconvGemmNHWC('T') (src/convGemm.c:71-76).
+ * dy: BF16 NHWC [b][ho][wo][kn8]; x: BF16 NHWC [b][h][w][c8]; dw: FP32 in the
+ * reference weight layout of `layout` (NHWC API [c][kh][kw][kn], NCHW API
+ * [kn][c][kh][kw]), overwritten. */
+convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_shape_t *shape, const void *dy,
+                                      const void *x, float *dw, void *workspace, size_t workspace_bytes,
+                                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,3 +123,60 @@ def test_dgrad_bf16_against_fp64(cglib, oracle_lib, shape):
     ref = O.dgrad_f64(C.NHWC, g, wt, dy)
     assert rel_max_rms(got, ref_r)[0] <= BF16_SELF_TOL
     assert rel_max_rms(got, ref)[0] <= BF16_TOL
+
+
+WGRAD_SHAPES = [
+    (2, 14, 14, 64, 64, 3, 1, 1, 1),      # kn < 128: X is the A operand, BN = 64
+    (2, 14, 14, 64, 128, 3, 1, 2, 1),     # dY is the A operand, BN = 256
+    (4, 7, 7, 256, 512, 1, 0, 1, 1),      # P = 196: ragged pixel chunks
+    (2, 20, 20, 3, 64, 7, 3, 2, 1),       # stem-like: channels padded to 8, Nx = 392
+    (1, 12, 10, 40, 96, 3, 2, 1, 2),      # kn = 96, dilation
+    (8, 28, 28, 128, 128, 3, 1, 1, 1),    # several pixel splits
+    (2, 9, 9, 16, 256, 1, 0, 2, 1),       # Nx = 16: BN = 64 on the X side
+]
+
+
+@pytest.mark.parametrize("shape", WGRAD_SHAPES, ids=[str(s) for s in WGRAD_SHAPES])
+def test_wgrad_bf16_against_fp64(cglib, oracle_lib, shape):
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, stride=stride, dil=dil)
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(11 + sum(shape))
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+    K = c * k * k
+    dws = []
+    for layout in (cg.NHWC, cg.NCHW, cg.NHWC):
+        dw = torch.full((K * kn,), float("nan"), device="cuda")
+        tc.wgrad_bf16(layout, s, dyd, xd, dw, ws)
+        dws.append(dw)
+    torch.cuda.synchronize()
+    cg.check_device()
+    assert torch.equal(dws[0], dws[2]), "weight gradient must be bit-reproducible"
+    got = dws[0].cpu().numpy()
+    ref_r = O.wgrad_f64(C.NHWC, g, bf16r(dy), bf16r(x))
+    ref = O.wgrad_f64(C.NHWC, g, dy, x)
+    assert rel_max_rms(got, ref_r)[0] <= 1e-4       # only FP32 accumulation differs
+    assert rel_max_rms(got, ref)[0] <= BF16_TOL
+    got_nchw = dws[1].cpu().numpy()
+    assert rel_max_rms(got_nchw, O.wgrad_f64(C.NCHW, g, np.ascontiguousarray(
+        bf16r(dy).reshape(b, s.ho, s.wo, kn).transpose(0, 3, 1, 2)).ravel(), np.ascontiguousarray(
+        bf16r(x).reshape(b, h, w, c).transpose(0, 3, 1, 2)).ravel()))[0] <= 1e-4
+
+
+def test_wgrad_bf16_rejects_small_workspace(cglib):
+    from convgemm_gb300 import tc
+    cg = cglib
+    s = cg.Shape.of(2, 8, 8, 64, 64, 3, 3, 1, 1)
+    ws = torch.empty(16, device="cuda")
+    x = torch.zeros(2, 8, 8, 64, dtype=torch.bfloat16, device="cuda")
+    dy = torch.zeros(2, 8, 8, 64, dtype=torch.bfloat16, device="cuda")
+    dw = torch.empty(64 * 9 * 64, device="cuda")
+    with pytest.raises(cg.ConvGemmError) as ei:
+        tc.wgrad_bf16(cg.NHWC, s, dy, x, dw, ws)
+    assert ei.value.status == 6
