@@ -1,0 +1,448 @@
+#!/usr/bin/env python3
+"""ResNet-50 conv fwd+bwd throughput on one GB300: BF16 tensor-core form vs FP32 plain.
+
+One step = for each of the 53 convolutions of ResNet-50 v1.5 at batch 64
+(224x224, NHWC): BN fold (FP64), weight packing, forward with the fused
+BN/ReLU epilogue, input gradient (not for the stem, whose input needs none)
+and weight gradient.  Inputs are synthetic, seeded, resident in HBM; the
+working set of a step (several GB) is far larger than L2.
+
+  value  : BF16 img/s, the step captured once in a CUDA graph and replayed;
+  e2e    : the same step through the public API call by call, with the
+           image batch and the top gradient copied host->device and all
+           weight gradients copied device->host inside every timed step;
+  fp32_plain : the same step with the FP32 plain kernels (the drop-in form);
+  roofline   : the dominant kernel family, CUDA-event timed, against
+           MEASURED_PEAKS.json;
+  cpu_baseline: the FP32 CPU restatement of the reference (oracle port) on
+           this host's cores, one image through all 53 layers.
+
+`--impl reference` times the reference's CPU path (the oracle port: the
+reference's sources are not on the GPU host) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from convgemm_gb300.workloads import conv_flops, out_hw, resnet50_layers  # noqa: E402
+
+METRIC = "ResNet-50 conv fwd+bwd img/s, BF16-TC vs FP32 plain on GB300 at stated rel err"
+BATCH = 64
+
+
+def c8(c):
+    return (c + 7) // 8 * 8
+
+
+def step_flops(layers, batch):
+    return sum(conv_flops(l, batch) * (2 if i == 0 else 3) for i, l in enumerate(layers))
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_baseline_run(layers, images, threads=None):
+    """The oracle port (FP32, the reference's summation order) on `images` images through all layers.
+    Returns (seconds, images)."""
+    import numpy as np
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    rng = np.random.default_rng(0)
+    t_total = 0.0
+    for i, l in enumerate(layers):
+        g = dict(b=images, h=l["h"], w=l["w"], c=l["c"], kn=l["kn"], kh=l["k"], kw=l["k"], vpad=l["pad"],
+                 hpad=l["pad"], vstr=l["stride"], hstr=l["stride"], vdil=1, hdil=1)
+        ho, wo = out_hw(l)
+        K = l["c"] * l["k"] * l["k"]
+        x = rng.standard_normal(images * l["h"] * l["w"] * l["c"]).astype(np.float32)
+        w = (rng.standard_normal(K * l["kn"]) * np.sqrt(2.0 / K)).astype(np.float32)
+        dy = rng.standard_normal(images * ho * wo * l["kn"]).astype(np.float32)
+        kn = l["kn"]
+        epi = {"mean": rng.normal(0, .1, kn).astype(np.float32), "inv_std": np.ones(kn, np.float32),
+               "gamma": np.ones(kn, np.float32), "beta": np.zeros(kn, np.float32), "bias": np.zeros(kn, np.float32),
+               "relu": True}
+        y = np.empty(images * ho * wo * kn, np.float32)
+        dw = np.empty(K * kn, np.float32)
+        dx = np.zeros_like(x)
+        t0 = time.perf_counter()
+        O.call_fwd("port", O.NHWC, g, w, x, y, epi)
+        if i > 0:
+            O.call_back("port", O.NHWC, g, w, dy, dx)
+        O.call_fwd("port", O.NHWC, g, dy, x, dw, None, trans="T")
+        t_total += time.perf_counter() - t0
+    return t_total, images
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    layers = resnet50_layers()
+    threads = os.cpu_count()
+    images = args.ref_images
+    for _ in range(args.warmup):
+        cpu_baseline_run(layers, images, threads)
+    times = []
+    for _ in range(args.steps):
+        t, n = cpu_baseline_run(layers, images, threads)
+        times.append(t)
+    tot = sum(times)
+    v = args.steps * images / tot
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "img/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "resnet50 v1.5 53 convs fwd+dgrad+wgrad, NHWC, FP32, CPU",
+                       "global_batch": images, "seq_len": None, "parallelism": "replicas"},
+            "cpu_baseline": {"value": v, "unit": "img/s", "cores": threads, "kind": "port",
+                             "sample": f"{images} image(s) x 53 layers fwd+wgrad+dgrad per step "
+                                       "(reference's KC=384 order, FP32)"},
+            "e2e": {"value": v, "unit": "img/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+class Net:
+    """Per-layer device buffers for both precision forms (synthetic, seeded)."""
+
+    def __init__(self, torch, cg, tc, layers, batch, with_fp32=True):
+        self.torch, self.cg, self.tc, self.layers, self.batch = torch, cg, tc, layers, batch
+        dev = "cuda"
+        g = torch.Generator(device=dev).manual_seed(20261203)
+        self.L = []
+        ws_bf16 = ws_f32 = 16
+        for i, l in enumerate(layers):
+            ho, wo = out_hw(l)
+            s = cg.Shape.of(batch, l["h"], l["w"], l["c"], l["kn"], l["k"], l["k"], l["pad"], l["pad"], l["stride"],
+                            l["stride"], 1, 1)
+            K = l["c"] * l["k"] * l["k"]
+            kn = l["kn"]
+            d = {"i": i, "s": s, "relu": not (l["name"].endswith("conv3") or l["name"].endswith("down")), "first": i == 0}
+            d["w32"] = torch.randn(K * kn, device=dev, generator=g) * (2.0 / K) ** 0.5
+            d["mean"] = torch.randn(kn, device=dev, generator=g) * 0.1
+            var = torch.rand(kn, device=dev, generator=g) * 1.5 + 0.5
+            d["inv_std"] = 1.0 / torch.sqrt(var + 1e-5)
+            d["gamma"] = torch.rand(kn, device=dev, generator=g) + 0.5
+            d["beta"] = torch.rand(kn, device=dev, generator=g) * 0.2 - 0.1
+            d["scale"] = torch.empty(kn, device=dev)
+            d["shift"] = torch.empty(kn, device=dev)
+            d["x"] = torch.randn(batch, l["h"], l["w"], c8(l["c"]), device=dev, generator=g).to(torch.bfloat16)
+            d["dy"] = (torch.randn(batch, ho, wo, c8(kn), device=dev, generator=g) * 0.1).to(torch.bfloat16)
+            d["y"] = torch.empty(batch, ho, wo, kn, device=dev, dtype=torch.bfloat16)
+            d["dx"] = None if i == 0 else torch.empty(batch, l["h"], l["w"], l["c"], device=dev, dtype=torch.bfloat16)
+            d["dw"] = torch.empty(K * kn, device=dev)
+            d["wp"] = torch.empty(tc.weights_size(s, tc.OPERAND_FWD) // 2, device=dev, dtype=torch.bfloat16)
+            d["wpd"] = None if i == 0 else torch.empty(tc.weights_size(s, tc.OPERAND_DGRAD) // 2, device=dev,
+                                                       dtype=torch.bfloat16)
+            ws_bf16 = max(ws_bf16, tc.wgrad_bf16_workspace_size(s))
+            if with_fp32:
+                ws_f32 = max(ws_f32, cg.wgrad_f32_workspace_size(s))
+            self.L.append(d)
+        self.ws = torch.empty(ws_bf16 // 4 + 1, device=dev)
+        self.ws32 = torch.empty(ws_f32 // 4 + 1, device=dev) if with_fp32 else None
+        self.with_fp32 = with_fp32
+        if with_fp32:
+            for d in self.L:
+                s = d["s"]
+                ho, wo = s.ho, s.wo
+                d["x32"] = torch.randn(batch, s.h, s.w, s.c, device=dev, generator=g)
+                d["dy32"] = torch.randn(batch, ho, wo, s.kn, device=dev, generator=g) * 0.1
+                d["y32"] = torch.empty(batch, ho, wo, s.kn, device=dev)
+                d["dx32"] = None if d["first"] else torch.empty(batch, s.h, s.w, s.c, device=dev)
+                d["dw32"] = torch.empty(s.c * s.kh * s.kw * s.kn, device=dev)
+
+    def launches_bf16(self):
+        # fold, pack fwd, fwd, [pack dgrad, dgrad], wgrad, wgrad reduce
+        return sum(5 if d["first"] else 7 for d in self.L)
+
+    def launches_f32(self):
+        return sum(3 if d["first"] else 4 for d in self.L)
+
+    def step_bf16(self, timers=None):
+        tc = self.tc
+        for d in self.L:
+            s = d["s"]
+            ev = timers.start("fwd", d) if timers else None
+            tc.fold_epilogue(s.kn, d["scale"], d["shift"], mean=d["mean"], inv_std=d["inv_std"], gamma=d["gamma"],
+                             beta=d["beta"])
+            tc.pack_weights(self.cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
+            if timers:
+                timers.mark(ev, "prep")
+            tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"])
+            if timers:
+                timers.mark(ev, "fwd")
+            if not d["first"]:
+                tc.pack_weights(self.cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
+                if timers:
+                    timers.mark(ev, "prep")
+                tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"])
+                if timers:
+                    timers.mark(ev, "dgrad")
+            tc.wgrad_bf16(self.cg.NHWC, s, d["dy"], d["x"], d["dw"], self.ws)
+            if timers:
+                timers.mark(ev, "wgrad")
+
+    def step_f32(self):
+        cg = self.cg
+        for d in self.L:
+            s = d["s"]
+            cg.fwd_f32(cg.NHWC, s, d["w32"], d["x32"], d["y32"], mean=d["mean"], inv_std=d["inv_std"],
+                       gamma=d["gamma"], beta=d["beta"], relu=d["relu"])
+            if not d["first"]:
+                cg.dgrad_f32(cg.NHWC, s, d["w32"], d["dy32"], d["dx32"], accumulate=False)
+            cg.wgrad_f32(cg.NHWC, s, d["dy32"], d["x32"], d["dw32"], self.ws32)
+
+
+class KernelTimers:
+    """CUDA events between consecutive launches of one (untimed) step, binned by kernel family."""
+
+    def __init__(self, torch):
+        self.torch = torch
+        self.rec = []
+
+    def start(self, kind, d):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record()
+        return {"last": e, "d": d}
+
+    def mark(self, ev, kind):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record()
+        self.rec.append((kind, ev["d"], ev["last"], e))
+        ev["last"] = e
+
+    def totals(self):
+        self.torch.cuda.synchronize()
+        out = {}
+        for kind, d, a, b in self.rec:
+            out.setdefault(kind, []).append((d, a.elapsed_time(b)))
+        return out
+
+
+def timed(torch, fn, steps, warmup, stream):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    end.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / steps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--fp32-steps", type=int, default=3)
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-images", type=int, default=1)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import convgemm_gb300 as cg
+    from convgemm_gb300 import tc
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cg.lib()
+    layers = resnet50_layers()
+    batch = args.batch
+    net = Net(torch, cg, tc, layers, batch, with_fp32=not args.no_fp32)
+    flops = step_flops(layers, batch)
+
+    # warm every launch path once outside any capture (attribute setup, error word)
+    net.step_bf16()
+    torch.cuda.synchronize()
+    cg.check_device()
+
+    # ---- value: the step as one CUDA graph
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        net.step_bf16()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=stream):
+            net.step_bf16()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    ms = timed(torch, graph.replay, args.steps, args.warmup, torch.cuda.current_stream())
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    cg.check_device()
+    value = world * batch / (ms / 1000.0)
+
+    # ---- per-kernel-family times of one eager step (untimed), for the roofline
+    timers = KernelTimers(torch)
+    net.step_bf16(timers)
+    fam = timers.totals()
+    peaks, peak_kind = read_peaks()
+    fam_summary = {}
+    for kind, recs in fam.items():
+        tms = sum(t for _, t in recs)
+        if kind in ("fwd", "dgrad", "wgrad"):
+            fl = sum(conv_flops(layers[d["i"]], batch) for d, _ in recs)
+        else:
+            fl = 0
+        fam_summary[kind] = {"ms": tms, "launches": len(recs), "tflops": (fl / (tms / 1000) / 1e12) if tms else 0}
+    dominant = max((k for k in fam_summary if k != "prep"), key=lambda k: fam_summary[k]["ms"])
+    dom = fam_summary[dominant]
+    kernel_name = {"fwd": "tc_conv_kernel (forward)", "dgrad": "tc_conv_kernel (input gradient)",
+                   "wgrad": "tc_wgrad_kernel + wgrad_reduce_kernel"}[dominant]
+    roofline = {"bound": "tensor", "kernel": kernel_name, "achieved": dom["tflops"],
+                "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                "frac": dom["tflops"] / peaks["bf16_tflops_sustained"], "traffic": None,
+                "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
+                "families": fam_summary}
+
+    # ---- e2e: public API call by call, host buffers in and out every step
+    img_host = torch.randn(batch, 224, 224, 3).pin_memory()
+    top_host = torch.randn(batch, 7, 7, 2048).pin_memory()
+    img_dev = torch.empty(batch, 224, 224, 3, device="cuda")
+    top_dev = torch.empty(batch, 7, 7, 2048, device="cuda")
+    dw_host = [torch.empty(d["dw"].numel()).pin_memory() for d in net.L]
+    h2d = img_host.numel() * 4 + top_host.numel() * 4
+    d2h = sum(t.numel() * 4 for t in dw_host)
+
+    def e2e_step():
+        img_dev.copy_(img_host, non_blocking=True)
+        top_dev.copy_(top_host, non_blocking=True)
+        tc.to_bf16_nhwc(cg.NHWC, batch, 3, 224, 224, img_dev, net.L[0]["x"])
+        tc.to_bf16_nhwc(cg.NHWC, batch, 2048, 7, 7, top_dev, net.L[-1]["dy"])
+        net.step_bf16()
+        for d, hbuf in zip(net.L, dw_host):
+            hbuf.copy_(d["dw"], non_blocking=True)
+
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1000 / e2e_steps
+    e2e = {"value": world * batch / (e2e_ms / 1000), "unit": "img/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+           "how": "python ctypes calls per layer on the current stream, no graph; pinned host buffers; "
+                  "wall clock around the steps with a device sync after the last"}
+
+    # ---- FP32 plain form
+    fp32 = None
+    if not args.no_fp32:
+        net.step_f32()
+        torch.cuda.synchronize()
+        cg.check_device()
+        ms32 = timed(torch, net.step_f32, args.fp32_steps, 1, torch.cuda.current_stream())
+        fp32 = {"value": world * batch / (ms32 / 1000), "unit": "img/s", "ms_per_step": ms32,
+                "tflops": flops / (ms32 / 1000) / 1e12}
+
+    # ---- CPU baseline (oracle port) on this host's cores, rank 0 only
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t, n = cpu_baseline_run(layers, 1, os.cpu_count())
+        cpu = {"value": n / t, "unit": "img/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "1 image x 53 layers fwd+wgrad+dgrad, FP32 in the reference's KC=384 order"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "img/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+                "config": {"workload": "resnet50 v1.5: 53 convs, fwd (folded BN + ReLU) + input grad (not stem) "
+                                       "+ weight grad, NHWC, BF16 tcgen05, FP32 accumulate",
+                           "global_batch": batch * world, "per_gpu_batch": batch, "seq_len": None,
+                           "parallelism": f"replicas{world}", "step": "one CUDA graph replay",
+                           "l2": "inputs larger than L2 (per-step working set of several GB)",
+                           "gflop_per_img": flops / batch / 1e9},
+                "tflops": flops / (ms / 1000) / 1e12,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "fp32_plain": fp32,
+                "bf16_vs_fp32": (value / fp32["value"]) if fp32 else None,
+                "clocks": clk, "gpu_launches": net.launches_bf16() * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -160,38 +160,46 @@ static void wgrad_core(const pdesc *d, int nchw, const float *dyt, const float *
     }
 }
 
-/* dx += scatter_k( sum_l dyt[p][l] * wt[l][k] ), one KC block of l at a time. */
+/* dx += scatter_k( sum_l dyt[p][l] * wt[l][k] ), one KC block of l at a time.
+ * Parallel over (image, input-channel chunk): the scatter targets of two
+ * tasks never overlap, so no atomics are needed and the order is fixed. */
 static void dgrad_core(const pdesc *d, int nchw, const float *wt, const float *dyt, float *dx) {
-    const int K = d->c * d->kh * d->kw, kn = d->kn;
+    const int K = d->c * d->kh * d->kw, kn = d->kn, T = d->kh * d->kw;
+    const int cchunk = d->c < 8 ? 1 : 8;
+    const int nchunks = (d->c + cchunk - 1) / cchunk;
     #pragma omp parallel
     {
-        float *blk = (float *) malloc(sizeof(float) * (size_t) K);
-        #pragma omp for schedule(dynamic, 1)
-        for (int b = 0; b < d->b; b++) {
-            for (int ox = 0; ox < d->ho; ox++)
-                for (int oy = 0; oy < d->wo; oy++) {
-                    int64_t p = ((int64_t) b * d->ho + ox) * d->wo + oy;
-                    const float *dr = dyt + (size_t) p * kn;
-                    for (int pc = 0; pc < kn; pc += CG_KC) {
-                        int kc = (kn - pc < CG_KC) ? kn - pc : CG_KC;
-                        for (int k = 0; k < K; k++) blk[k] = 0.0f;
-                        for (int l = pc; l < pc + kc; l++) {
-                            const float dv = dr[l];
-                            const float *wr = wt + (size_t) l * K;
-                            for (int k = 0; k < K; k++) blk[k] = fmaf(wr[k], dv, blk[k]);
-                        }
-                        for (int k = 0; k < K; k++) {
-                            int ky = k % d->kw, kx = (k / d->kw) % d->kh, c = k / (d->kw * d->kh);
-                            int ix = d->vstr * ox + d->vdil * kx - d->vpad;
-                            int iy = d->hstr * oy + d->hdil * ky - d->hpad;
-                            if (ix < 0 || ix >= d->h || iy < 0 || iy >= d->w) continue;
-                            size_t o = nchw ? ((((size_t) b * d->c + c) * d->h + ix) * d->w + iy)
-                                            : ((((size_t) b * d->h + ix) * d->w + iy) * d->c + c);
-                            dx[o] += blk[k];
+        float *blk = (float *) malloc(sizeof(float) * (size_t) cchunk * T);
+        #pragma omp for schedule(dynamic, 1) collapse(2)
+        for (int b = 0; b < d->b; b++)
+            for (int cc = 0; cc < nchunks; cc++) {
+                const int c0 = cc * cchunk, c1 = (c0 + cchunk < d->c) ? c0 + cchunk : d->c;
+                const int k0 = c0 * T, nk = (c1 - c0) * T;
+                for (int ox = 0; ox < d->ho; ox++)
+                    for (int oy = 0; oy < d->wo; oy++) {
+                        int64_t p = ((int64_t) b * d->ho + ox) * d->wo + oy;
+                        const float *dr = dyt + (size_t) p * kn;
+                        for (int pc = 0; pc < kn; pc += CG_KC) {
+                            int kc = (kn - pc < CG_KC) ? kn - pc : CG_KC;
+                            for (int k = 0; k < nk; k++) blk[k] = 0.0f;
+                            for (int l = pc; l < pc + kc; l++) {
+                                const float dv = dr[l];
+                                const float *wr = wt + (size_t) l * K + k0;
+                                for (int k = 0; k < nk; k++) blk[k] = fmaf(wr[k], dv, blk[k]);
+                            }
+                            for (int kk = 0; kk < nk; kk++) {
+                                int k = k0 + kk;
+                                int ky = k % d->kw, kx = (k / d->kw) % d->kh, c = k / (d->kw * d->kh);
+                                int ix = d->vstr * ox + d->vdil * kx - d->vpad;
+                                int iy = d->hstr * oy + d->hdil * ky - d->hpad;
+                                if (ix < 0 || ix >= d->h || iy < 0 || iy >= d->w) continue;
+                                size_t o = nchw ? ((((size_t) b * d->c + c) * d->h + ix) * d->w + iy)
+                                                : ((((size_t) b * d->h + ix) * d->w + iy) * d->c + c);
+                                dx[o] += blk[kk];
+                            }
                         }
                     }
-                }
-        }
+            }
         free(blk);
     }
 }
