@@ -105,6 +105,7 @@ def lib():
         L.convgemm_wgrad_bf16_workspace_size.argtypes = [SP]
         L.convgemm_wgrad_bf16_workspace_size.restype = ctypes.c_size_t
         L.convgemm_wgrad_bf16.argtypes = [_I, SP, _VP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
+        L.convgemm_wgrad_bf16_noalloc.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         _lib = L
     return _lib
 

@@ -137,6 +137,18 @@ convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_s
                                       const void *x, float *dw, void *workspace, size_t workspace_bytes,
                                       void *stream);
 
+/* Weight gradient like convgemm_wgrad_bf16, for callers that cannot allocate GPU
+ * memory (e.g. code running inside a CUDA-graph stream capture, where cudaMalloc
+ * is not allowed, or services that fix their memory footprint at start-up): it
+ * takes no workspace and calls no allocator.  No counterpart in the reference.
+ * Its split partials live in one file-scope device array of 16 MiB (4 Mi FP32
+ * values) that every GPU loading the library keeps until exit; layers with
+ * kh*kw*c8*kn above that are rejected with CONVGEMM_ERROR_NOT_SUPPORTED.  All
+ * calls share the array, so calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's address; make it before any stream capture. */
+convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                              const void *dy, const void *x, float *dw, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
