@@ -281,6 +281,68 @@ class KernelTimers:
         return out
 
 
+def layer_bytes(l, batch, elem=2):
+    ho, wo = out_hw(l)
+    return elem * (batch * l["h"] * l["w"] * c8(l["c"]) + batch * ho * wo * l["kn"]) + \
+        elem * l["c"] * l["k"] * l["k"] * l["kn"]
+
+
+def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
+    """CUDA-event time of each BF16 op of each layer (reps back to back), with its roofline bound."""
+    tc, cg = net.tc, net.cg
+    rows = []
+    pk_t = peaks["bf16_tflops_sustained"] * 1e12
+    pk_b = peaks["hbm_gbs"] * 1e9
+    for d, l in zip(net.L, layers):
+        s = d["s"]
+        ops = {"fwd": lambda: tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"]),
+               "wgrad": lambda: tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], net.ws)}
+        if not d["first"]:
+            ops["dgrad"] = lambda: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"])
+        fl = conv_flops(l, batch)
+        by = layer_bytes(l, batch)
+        row = {"layer": l["name"], "shape": [l["h"], l["c"], l["kn"], l["k"], l["stride"]], "gflop": fl / 1e9,
+               "mb": by / 1e6, "roofline_us": max(fl / pk_t, by / pk_b) * 1e6}
+        for name, fn in ops.items():
+            fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(reps):
+                fn()
+            b.record()
+            torch.cuda.synchronize()
+            us = a.elapsed_time(b) * 1000 / reps
+            row[name + "_us"] = us
+            row[name + "_frac"] = row["roofline_us"] / us
+        rows.append(row)
+    with open(path, "w") as f:
+        json.dump(rows, f, indent=1)
+
+
+def run_only(torch, cg, tc, layers, batch, args):
+    name, op = args.only.split(":")
+    idx = next(i for i, l in enumerate(layers) if l["name"] == name)
+    net = Net(torch, cg, tc, [layers[idx]], batch, with_fp32=False)
+    d = net.L[0]
+    d["first"] = False
+    s = d["s"]
+    if d["wpd"] is None:
+        d["wpd"] = torch.empty(tc.weights_size(s, tc.OPERAND_DGRAD) // 2, device="cuda", dtype=torch.bfloat16)
+        d["dx"] = torch.empty(batch, s.h, s.w, s.c, device="cuda", dtype=torch.bfloat16)
+    tc.fold_epilogue(s.kn, d["scale"], d["shift"], mean=d["mean"], inv_std=d["inv_std"], gamma=d["gamma"],
+                     beta=d["beta"])
+    tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
+    tc.pack_weights(cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
+    fn = {"fwd": lambda: tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"]),
+          "dgrad": lambda: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"]),
+          "wgrad": lambda: tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], net.ws)}[op]
+    ms = timed(torch, fn, args.steps, args.warmup, torch.cuda.current_stream())
+    cg.check_device()
+    fl = conv_flops(layers[idx], batch)
+    print(json.dumps({"only": args.only, "batch": batch, "us": ms * 1000, "tflops": fl / (ms / 1000) / 1e12}))
+
+
 def timed(torch, fn, steps, warmup, stream):
     for _ in range(warmup):
         fn()
@@ -305,6 +367,11 @@ def main():
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-images", type=int, default=1)
+    ap.add_argument("--per-layer", default=None,
+                    help="write a per-layer table (forward / input grad / weight grad times) to this JSON file")
+    ap.add_argument("--only", default=None,
+                    help="LAYER:OP (e.g. s3b2_conv2:fwd): run just that BF16 op, eagerly, warmup+steps times "
+                         "(for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -324,6 +391,8 @@ def main():
     cg.lib()
     layers = resnet50_layers()
     batch = args.batch
+    if args.only:
+        return run_only(torch, cg, tc, layers, batch, args)
     net = Net(torch, cg, tc, layers, batch, with_fp32=not args.no_fp32)
     flops = step_flops(layers, batch)
 
@@ -375,6 +444,9 @@ def main():
                 "frac": dom["tflops"] / peaks["bf16_tflops_sustained"], "traffic": None,
                 "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
                 "families": fam_summary}
+
+    if args.per_layer and rank == 0:
+        per_layer_table(torch, net, layers, batch, peaks, args.per_layer)
 
     # ---- e2e: public API call by call, host buffers in and out every step
     img_host = torch.randn(batch, 224, 224, 3).pin_memory()
