@@ -5,23 +5,27 @@
 // computes in gather form: every input-gradient pixel collects the taps that
 // reach it, so there is no col2im/row2im scatter (src/im2row_nhwc.c:231-267)
 // and no atomics.  A stride > 1 input gradient is split into stride-phase
-// classes (pixels with the same (ih + pad) mod stride see the same taps), one
-// per blockIdx.z, each a dense implicit GEMM of its own.
+// classes (pixels with the same (ih + pad) mod stride see the same taps), each
+// a dense implicit GEMM of its own; their tiles share one launch.
 //
 // GEMM view of one class: D[m, n] = sum_k A[m, k] * B[n, k]
-//   m = output pixel of the class (128 per CTA),
-//   n = output channel (BN per CTA, in TMEM columns),
+//   m = output pixel of the class (128 per tile),
+//   n = output channel (BN per tile, in TMEM columns),
 //   k = tap * Cin + ci over the class's taps (64 per pipeline stage).
 // A is gathered from the NHWC activation with 16-byte cp.async (zero-filled
 // for padding) straight into the 128-byte-swizzled K-major layout the tensor
 // core reads — no im2row buffer exists anywhere.  B is the packed weight
-// matrix [Cout][K] loaded by TMA.  The FP32 accumulator lives in TMEM and the
-// epilogue (per-channel scale/shift = folded bias + batch-norm, ReLU, BF16
-// cast) runs TMEM -> registers -> global.
+// matrix [Cout][K] loaded by TMA.  The FP32 accumulator lives in TMEM.
 //
-// Warp roles (160 threads): warps 0-3 gather A (thread 0 also issues the B
-// TMA) and afterwards drain TMEM (warp w owns TMEM lanes 32w..32w+31); warp 4
-// allocates TMEM and one lane issues the MMAs.
+// The kernel is persistent: each CTA walks tiles blockIdx.x, +gridDim.x, ...
+// with two TMEM accumulators, so the epilogue of one tile runs while the MMAs
+// of the next accumulate.  Warp roles (288 threads):
+//   warps 0-3  gather A (thread 0 also issues the B TMA), stage ring of STAGES;
+//   warps 4-7  epilogue: TMEM -> registers (tcgen05.ld), scale/shift/ReLU,
+//              BF16, then either a 128-byte-swizzled shared-memory tile and a
+//              TMA store (pixels contiguous in the output), or direct stores
+//              (the strided pixels of an input-gradient class);
+//   warp 8     allocates TMEM; one lane issues tcgen05.mma and the commits.
 #include <cuda_bf16.h>
 
 #include "cg_common.cuh"
@@ -38,8 +42,10 @@ struct TcCfg {
     static constexpr uint32_t A_BYTES = BM * BK * 2;
     static constexpr uint32_t B_BYTES = BN * BK * 2;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-    static constexpr int LAG = STAGES - 1;  // cp.async groups kept in flight per producer thread
-    static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
+    static constexpr uint32_t EPI_BYTES = BM * 64 * 2;  // one 128 x 64 BF16 output chunk
+    static constexpr int LAG = STAGES - 1;              // cp.async groups in flight per producer thread
+    static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256;
+    static constexpr int THREADS = 288;
 };
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -47,19 +53,48 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(160, 1)
-    tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap) {
-    using C = TcCfg<BN, STAGES>;
-    const TcClass &cl = p.cls[blockIdx.z];
-    if ((int) blockIdx.x >= cl.mtiles) return;
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"((uint64_t) map),
+                 "r"(src), "r"(x), "r"(y)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+struct Tile {
+    int cls, m0, n0;
+};
+
+__device__ __forceinline__ Tile decode_tile(const TcConvParams &p, int t) {
+    int c = 0;
+    while (c + 1 < p.ncls && t >= p.cls[c + 1].tile0) c++;
+    const int local = t - p.cls[c].tile0;
+    Tile tl;
+    tl.cls = c;
+    tl.m0 = (local / p.ntiles) * 128;
+    tl.n0 = (local % p.ntiles) * p.bn;
+    return tl;
+}
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(288, 1)
+    tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
+                   const __grid_constant__ CUtensorMap omap) {
+    using C = TcCfg<BN, STAGES>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-    uint64_t *full = (uint64_t *) (base + STAGES * C::STAGE_BYTES);
+    uint8_t *epi_smem = base + STAGES * C::STAGE_BYTES;
+    uint64_t *full = (uint64_t *) (epi_smem + 2 * C::EPI_BYTES);
     uint64_t *empty = full + STAGES;
-    uint64_t *accum = empty + STAGES;
-    uint32_t *tmem_holder = (uint32_t *) (accum + 1);
+    uint64_t *acc_full = empty + STAGES;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tmem_holder = (uint32_t *) (acc_empty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -67,152 +102,213 @@ __global__ void __launch_bounds__(160, 1)
             tc::mbar_init(&full[s], 128 + 1);
             tc::mbar_init(&empty[s], 1);
         }
-        tc::mbar_init(accum, 1);
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], 128);
+        }
         tc::fence_mbar_init();
         tc::prefetch_tmap(&wmap);
+        if (p.epi_tma) tc::prefetch_tmap(&omap);
     }
-    if (warp == 4) {
-        tc::tmem_alloc(tmem_holder, BN);
+    if (warp == 8) {
+        tc::tmem_alloc(tmem_holder, 2 * BN);
         tc::tmem_relinquish();
     }
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_holder;
-
-    const int m0 = blockIdx.x * C::BM, n0 = blockIdx.y * BN;
-    const int M = p.B * cl.Hg * cl.Wg;
-    const int KT = cl.ktiles;
     bool ok = true;
 
     if (warp < 4) {
-        // ------------------------------------------------ producer: gather A
+        // ------------------------------------------------ producers: gather A, TMA B
         const int t = threadIdx.x;
         const int piece = t & 7;   // 16-byte piece of the 128-byte K row
         const int r0 = t >> 3;     // rows r0 + 16*i
-        int rb[8], ry[8], rx[8];
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int m = m0 + r0 + 16 * i;
-            if (m < M) {
-                uint32_t q, jw, j, b;
-                cl.dwg.divmod(m, q, jw);
-                cl.dhg.divmod(q, b, j);
-                rb[i] = b;
-                ry[i] = (int) j * cl.isy + cl.iby;
-                rx[i] = (int) jw * cl.isx + cl.ibx;
-            } else {
-                rb[i] = -1;
-                ry[i] = rx[i] = 0;
-            }
-        }
-        for (int kt = 0; kt < KT; kt++) {
-            const int s = kt % STAGES;
-            const uint32_t ph = (kt / STAGES) & 1;
-            if (kt >= STAGES) ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1);
-            if (!ok) break;
-            const int k = kt * C::BK + piece * 8;
-            uint32_t tap, ci;
-            p.dcin.divmod(k, tap, ci);
-            const bool kval = (int) tap < cl.ntaps;
-            const int oy = kval ? cl.toy[tap] : 0, ox = kval ? cl.tox[tap] : 0;
-            const uint32_t sA = tc::smem_u32(base + s * C::STAGE_BYTES);
+        uint32_t it = 0;
+        for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
+            const Tile tl = decode_tile(p, tile);
+            const TcClass &cl = p.cls[tl.cls];
+            const int M = p.B * cl.Hg * cl.Wg;
+            int rb[8], ry[8], rx[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) {
-                const int r = r0 + 16 * i;
-                const int iy = ry[i] + oy, ix = rx[i] + ox;
-                const bool v = kval && rb[i] >= 0 && (unsigned) iy < (unsigned) p.Hin && (unsigned) ix < (unsigned) p.Win;
-                const bf16 *src = v ? p.in + ((((size_t) rb[i] * p.Hin + iy) * p.Win + ix) * p.Cin + ci) : p.in;
-                tc::cp_async_16(sA + r * 128 + ((piece ^ (r & 7)) << 4), src, v ? 16u : 0u);
+                const int m = tl.m0 + r0 + 16 * i;
+                if (m < M) {
+                    uint32_t q, jw, j, b;
+                    cl.dwg.divmod(m, q, jw);
+                    cl.dhg.divmod(q, b, j);
+                    rb[i] = b;
+                    ry[i] = (int) j * cl.isy + cl.iby;
+                    rx[i] = (int) jw * cl.isx + cl.ibx;
+                } else {
+                    rb[i] = -1;
+                    ry[i] = rx[i] = 0;
+                }
             }
-            tc::cp_async_commit();
-            if (t == 0) {
-                tc::mbar_arrive_expect_tx(&full[s], C::B_BYTES);
-                tc::tma_load_2d(tc::smem_u32(base + s * C::STAGE_BYTES + C::A_BYTES), &wmap, cl.kbeg + kt * C::BK,
-                                n0, &full[s]);
-            }
-            if (kt >= C::LAG) {
-                tc::cp_async_wait<C::LAG>();
-                tc::fence_proxy_async_smem();
-                tc::mbar_arrive(&full[(kt - C::LAG) % STAGES]);
+            for (int kt = 0; kt < cl.ktiles; kt++, it++) {
+                const int s = it % STAGES;
+                const uint32_t ph = (it / STAGES) & 1;
+                if (it >= (uint32_t) STAGES) ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1);
+                if (!ok) break;
+                const int k = kt * C::BK + piece * 8;
+                uint32_t tap, ci;
+                p.dcin.divmod(k, tap, ci);
+                const bool kval = (int) tap < cl.ntaps;
+                const int oy = kval ? cl.toy[tap] : 0, ox = kval ? cl.tox[tap] : 0;
+                const uint32_t sA = tc::smem_u32(base + s * C::STAGE_BYTES);
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const int r = r0 + 16 * i;
+                    const int iy = ry[i] + oy, ix = rx[i] + ox;
+                    const bool v =
+                        kval && rb[i] >= 0 && (unsigned) iy < (unsigned) p.Hin && (unsigned) ix < (unsigned) p.Win;
+                    const bf16 *src = v ? p.in + ((((size_t) rb[i] * p.Hin + iy) * p.Win + ix) * p.Cin + ci) : p.in;
+                    tc::cp_async_16(sA + r * 128 + ((piece ^ (r & 7)) << 4), src, v ? 16u : 0u);
+                }
+                tc::cp_async_commit();
+                if (t == 0) {
+                    tc::mbar_arrive_expect_tx(&full[s], C::B_BYTES);
+                    tc::tma_load_2d(tc::smem_u32(base + s * C::STAGE_BYTES + C::A_BYTES), &wmap,
+                                    cl.kbeg + kt * C::BK, tl.n0, &full[s]);
+                }
+                if (it >= (uint32_t) C::LAG) {
+                    tc::cp_async_wait<C::LAG>();
+                    tc::fence_proxy_async_smem();
+                    tc::mbar_arrive(&full[(it - C::LAG) % STAGES]);
+                }
             }
         }
         tc::cp_async_wait<0>();
         tc::fence_proxy_async_smem();
         if (ok)
-            for (int kt = (KT > C::LAG ? KT - C::LAG : 0); kt < KT; kt++) tc::mbar_arrive(&full[kt % STAGES]);
-
+            for (uint32_t j = (it > (uint32_t) C::LAG ? it - C::LAG : 0); j < it; j++) tc::mbar_arrive(&full[j % STAGES]);
+    } else if (warp < 8) {
         // ------------------------------------------------ epilogue
-        if (ok) ok = tc::mbar_wait(accum, 0, p.err, 3);
-        tc::tc_fence_after();
-        const int row = warp * 32 + lane;
-        const int m = m0 + row;
-        bf16 *orow = nullptr;
-        if (m < M) {
-            uint32_t q, jw, j, b;
-            cl.dwg.divmod(m, q, jw);
-            cl.dhg.divmod(q, b, j);
-            const int oy = cl.oy0 + cl.osy * (int) j, ox = cl.ox0 + cl.osx * (int) jw;
-            orow = p.out + (((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout;
-        }
-        if (ok) {
+        const int ew = warp - 4;          // TMEM lane quarter
+        const int row = ew * 32 + lane;   // tile row = TMEM lane
+        const int et = threadIdx.x - 128; // 0..127
+        uint32_t lt = 0;                  // local tile count
+        int ebuf = 0;                     // staging buffer toggle
+        for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
+            const Tile tl = decode_tile(p, tile);
+            const TcClass &cl = p.cls[tl.cls];
+            const int M = p.B * cl.Hg * cl.Wg;
+            const int buf = lt & 1;
+            ok = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 3);
+            if (!ok) break;
+            tc::tc_fence_after();
+            const int m = tl.m0 + row;
+            bf16 *orow = nullptr;
+            if (!p.epi_tma && m < M) {
+                uint32_t q, jw, j, b;
+                cl.dwg.divmod(m, q, jw);
+                cl.dhg.divmod(q, b, j);
+                const int oy = cl.oy0 + cl.osy * (int) j, ox = cl.ox0 + cl.osx * (int) jw;
+                orow = p.out + (((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout;
+            }
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                uint32_t v[32];
-                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+            for (int c0 = 0; c0 < BN; c0 += 64) {
+                uint32_t v0[32], v1[32];
+                const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) (buf * BN + c0);
+                tc::tmem_ld_32x32b_x32(ta, v0);
+                tc::tmem_ld_32x32b_x32(ta + 32, v1);
                 tc::tmem_ld_wait();
-                const int nb = n0 + c0;
-                if (orow && nb < p.Cout) {
-                    float f[32];
+                if (c0 + 64 >= BN) {
+                    // the whole accumulator is in registers: hand the TMEM buffer back to the MMA warp
+                    tc::tc_fence_before();
+                    tc::mbar_arrive(&acc_empty[buf]);
+                }
+                const int nb = tl.n0 + c0;
+                uint32_t pk[32];
 #pragma unroll
-                    for (int jj = 0; jj < 32; jj++) {
-                        const int n = min(nb + jj, p.Cout - 1);
-                        float a = __uint_as_float(v[jj]);
-                        if (p.scale) a = a * __ldg(p.scale + n);
-                        if (p.shift) a = a + __ldg(p.shift + n);
-                        if (p.relu) a = fmaxf(a, 0.0f);
-                        f[jj] = a;
+                for (int jj = 0; jj < 32; jj++) {
+                    const int n0 = min(nb + 2 * jj, p.Cout - 1), n1 = min(nb + 2 * jj + 1, p.Cout - 1);
+                    float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
+                    float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
+                    if (p.scale) {
+                        a *= __ldg(p.scale + n0);
+                        b *= __ldg(p.scale + n1);
                     }
-                    if (nb + 32 <= p.Cout) {
+                    if (p.shift) {
+                        a += __ldg(p.shift + n0);
+                        b += __ldg(p.shift + n1);
+                    }
+                    if (p.relu) {
+                        a = fmaxf(a, 0.0f);
+                        b = fmaxf(b, 0.0f);
+                    }
+                    pk[jj] = pack_bf16x2(a, b);
+                }
+                if (p.epi_tma) {
+                    // 128 x 64 chunk through shared memory, stored by TMA (out-of-range rows/columns clipped)
+                    if (et == 0) bulk_wait_read<1>();
+                    epi_bar();
+                    uint8_t *stg = epi_smem + ebuf * C::EPI_BYTES;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        uint4 u = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+                        *reinterpret_cast<uint4 *>(stg + row * 128 + ((q ^ (row & 7)) << 4)) = u;
+                    }
+                    tc::fence_proxy_async_smem();
+                    epi_bar();
+                    if (et == 0 && nb < p.Cout) {
+                        tma_store_2d(&omap, tc::smem_u32(stg), nb, tl.m0);
+                        bulk_commit();
+                    }
+                    ebuf ^= 1;
+                } else if (orow && nb < p.Cout) {
+                    if (nb + 64 <= p.Cout) {
                         uint4 *dst = reinterpret_cast<uint4 *>(orow + nb);
 #pragma unroll
-                        for (int q4 = 0; q4 < 4; q4++) {
-                            uint4 u;
-                            u.x = pack_bf16x2(f[q4 * 8 + 0], f[q4 * 8 + 1]);
-                            u.y = pack_bf16x2(f[q4 * 8 + 2], f[q4 * 8 + 3]);
-                            u.z = pack_bf16x2(f[q4 * 8 + 4], f[q4 * 8 + 5]);
-                            u.w = pack_bf16x2(f[q4 * 8 + 6], f[q4 * 8 + 7]);
-                            dst[q4] = u;
-                        }
+                        for (int q = 0; q < 8; q++) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
                     } else {
-                        for (int jj = 0; jj < 32 && nb + jj < p.Cout; jj++) orow[nb + jj] = __float2bfloat16_rn(f[jj]);
+#pragma unroll
+                        for (int jj = 0; jj < 32; jj++) {
+                            __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&pk[jj]);
+                            if (nb + 2 * jj < p.Cout) orow[nb + 2 * jj] = h.x;
+                            if (nb + 2 * jj + 1 < p.Cout) orow[nb + 2 * jj + 1] = h.y;
+                        }
                     }
                 }
             }
         }
+        if (et == 0) bulk_wait_all();
     } else {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
-            for (int kt = 0; kt < KT; kt++) {
-                const int s = kt % STAGES;
-                const uint32_t ph = (kt / STAGES) & 1;
-                if (!tc::mbar_wait(&full[s], ph, p.err, 2)) {
-                    ok = false;
-                    break;
+            uint32_t it = 0, lt = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
+                const Tile tl = decode_tile(p, tile);
+                const int KT = p.cls[tl.cls].ktiles;
+                const int buf = lt & 1;
+                if (lt >= 2) {
+                    ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) - 1) & 1, p.err, 4);
+                    if (!ok) break;
+                    tc::tc_fence_after();
                 }
-                tc::tc_fence_after();
-                const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
-                const uint32_t b0 = a0 + C::A_BYTES;
+                const uint32_t dt = tmem + (uint32_t) (buf * BN);
+                for (int kt = 0; kt < KT; kt++, it++) {
+                    const int s = it % STAGES;
+                    const uint32_t ph = (it / STAGES) & 1;
+                    if (!tc::mbar_wait(&full[s], ph, p.err, 2)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
+                    const uint32_t b0 = a0 + C::A_BYTES;
 #pragma unroll
-                for (int k = 0; k < C::BK / 16; k++) {
-                    const uint64_t ad = tc::sw128_desc(a0 + k * 32, 16, 1024);
-                    const uint64_t bd = tc::sw128_desc(b0 + k * 32, 16, 1024);
-                    tc::mma_f16(tmem, ad, bd, idesc, (kt | k) != 0);
+                    for (int k = 0; k < C::BK / 16; k++) {
+                        const uint64_t ad = tc::sw128_desc(a0 + k * 32, 16, 1024);
+                        const uint64_t bd = tc::sw128_desc(b0 + k * 32, 16, 1024);
+                        tc::mma_f16(dt, ad, bd, idesc, (kt | k) != 0);
+                    }
+                    tc::mma_commit(&empty[s]);
                 }
-                tc::mma_commit(&empty[s]);
+                tc::mma_commit(&acc_full[buf]);
             }
-            tc::mma_commit(accum);
         }
         __syncwarp();
     }
@@ -220,11 +316,12 @@ __global__ void __launch_bounds__(160, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 4) tc::tmem_dealloc(tmem, BN);
+    if (warp == 8) tc::tmem_dealloc(tmem, 2 * BN);
 }
 
 template <int BN, int STAGES>
-cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &map, dim3 grid, cudaStream_t st) {
+cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
+                      cudaStream_t st) {
     using C = TcCfg<BN, STAGES>;
     auto kern = tc_conv_kernel<BN, STAGES>;
     static bool attr = false;
@@ -233,19 +330,18 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &map, dim3 grid, 
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, 160, C::SMEM, st>>>(p, map);
+    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &map, int bn, int mtiles_max, int ntiles,
+cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
                            cudaStream_t st) {
-    dim3 grid(mtiles_max, ntiles, p.ncls);
-    switch (bn) {
-        case 64: return launch_bn<64, 4>(p, map, grid, st);    // 97 KB: two CTAs per SM
-        case 128: return launch_bn<128, 3>(p, map, grid, st);  // 97 KB: two CTAs per SM
-        case 256: return launch_bn<256, 4>(p, map, grid, st);
+    switch (p.bn) {
+        case 64: return launch_bn<64, 8>(p, wmap, omap, grid, st);
+        case 128: return launch_bn<128, 6>(p, wmap, omap, grid, st);
+        case 256: return launch_bn<256, 4>(p, wmap, omap, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -20,6 +20,7 @@ struct TcClass {
     int kbeg;    // first K column of this class in the packed weights (multiple of 64)
     int ktiles;  // K / 64
     int mtiles;  // ceil(B*Hg*Wg / 128)
+    int tile0;   // index of the class's first tile in the launch (classes' tiles are concatenated)
     FastDiv dwg, dhg;
     int16_t toy[TC_MAXTAPS], tox[TC_MAXTAPS];
 };
@@ -33,9 +34,14 @@ struct TcConvParams {
     int B, Hin, Win, Cin, Hout, Wout, Cout;
     FastDiv dcin;
     int *err;                  // device error word for timed-out waits
+    int bn;                    // output channels per tile (64, 128, 256)
+    int ntiles;                // tiles along the output channels
+    int ntiles_total;          // all tiles of all classes; tile t of a class: m = t / ntiles, n = t % ntiles
+    int epi_tma;               // output pixels are the GEMM rows in order: stage in SMEM, TMA store
     int ncls;
     TcClass cls[TC_MAXCLS];
 };
 
-cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &map, int bn, int mtiles_max, int ntiles,
+// wmap: packed weights [Cout][K] (box 64 x bn); omap: output [pixels][Cout] (box 64 x 128), used when epi_tma.
+cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
                            cudaStream_t st);

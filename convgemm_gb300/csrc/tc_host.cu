@@ -170,15 +170,56 @@ PackDgradInfo tc_pack_info(const TcPlan &pl) {
     return info;
 }
 
+int tc_num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 148;
+        n = v;
+    }
+    return n;
+}
+
+// Output channels per tile: fewest waves of tiles times the per-stage cost of a
+// tile (the 16 KB A gather bounds a stage at ~128 cycles; the MMA takes 2*BN).
+int tc_pick_bn(const TcPlan &pl, int sms) {
+    int best = 64;
+    long long best_cost = -1;
+    for (int bn : {256, 128, 64}) {
+        if (bn > 64 && bn / 2 >= pl.Cout) continue;
+        long long tiles = 0;
+        for (int c = 0; c < pl.ncls; c++) tiles += (long long) pl.cls[c].mtiles * ((pl.Cout + bn - 1) / bn);
+        const long long waves = (tiles + sms - 1) / sms;
+        const long long cost = waves * (bn * 2 > 128 ? bn * 2 : 128);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = bn;
+        }
+    }
+    return best;
+}
+
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
-    CUtensorMap map;
-    if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wpacked, pl.Cout, pl.Ktot, 64,
-                                             pl.bn))
-        return e;
+    const int sms = tc_num_sms();
     TcConvParams p;
     memset(&p, 0, sizeof(p));
+    p.bn = tc_pick_bn(pl, sms);
+    CUtensorMap wmap, omap;
+    if (convgemm_status_t e =
+            tc_make_map_2d(&wmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wpacked, pl.Cout, pl.Ktot, 64, p.bn))
+        return e;
+    const TcClass &c0 = pl.cls[0];
+    p.epi_tma = pl.ncls == 1 && c0.osy == 1 && c0.osx == 1 && c0.oy0 == 0 && c0.ox0 == 0 && c0.Hg == pl.Hout &&
+                c0.Wg == pl.Wout && (pl.Cout % 8) == 0 && ((uintptr_t) out & 15) == 0;
+    memset(&omap, 0, sizeof(omap));
+    if (p.epi_tma) {
+        if (convgemm_status_t e = tc_make_map_2d(&omap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, out,
+                                                 (long long) s.b * pl.Hout * pl.Wout, pl.Cout, 64, 128))
+            return e;
+    }
     p.in = (const __nv_bfloat16 *) in;
     p.out = (__nv_bfloat16 *) out;
     p.scale = scale;
@@ -194,10 +235,17 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     p.dcin = FastDiv(pl.Cin);
     p.err = cg_device_error_word();
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
+    p.ntiles = (pl.Cout + p.bn - 1) / p.bn;
     p.ncls = pl.ncls;
-    for (int c = 0; c < pl.ncls; c++) p.cls[c] = pl.cls[c];
-    const int ntiles = (pl.Cout + pl.bn - 1) / pl.bn;
-    return cg_cuda_check(tc_conv_launch(p, map, pl.bn, pl.mtiles_max, ntiles, st), "tensor-core conv launch");
+    int t0 = 0;
+    for (int c = 0; c < pl.ncls; c++) {
+        p.cls[c] = pl.cls[c];
+        p.cls[c].tile0 = t0;
+        t0 += pl.cls[c].mtiles * p.ntiles;
+    }
+    p.ntiles_total = t0;
+    const int grid = t0 < sms ? t0 : sms;
+    return cg_cuda_check(tc_conv_launch(p, wmap, omap, grid, st), "tensor-core conv launch");
 }
 
 // ------------------------------------------------------------ public API
