@@ -43,7 +43,9 @@ struct TcCfg {
     static constexpr uint32_t B_BYTES = BN * BK * 2;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t EPI_BYTES = BM * 64 * 2;  // one 128 x 64 BF16 output chunk
-    static constexpr int LAG = STAGES - 1;              // cp.async groups in flight per producer thread
+    // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
+    // MMA run ahead of the arrivals (LAG = STAGES - 1 would lock the two in step)
+    static constexpr int LAG = STAGES / 2;
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256;
     static constexpr int THREADS = 288;
 };

@@ -33,7 +33,7 @@ struct WgCfg {
     static constexpr int X_ATOMS = (XA ? BM : BN) / 64;    // 64-channel atoms gathered from X
     static constexpr int DY_ATOMS = (XA ? BN : BM) / 64;   // 64-channel atoms loaded from dY
     static constexpr uint32_t DY_BYTES = DY_ATOMS * 64 * BK * 2;
-    static constexpr int LAG = STAGES - 1;
+    static constexpr int LAG = STAGES / 2;  // half the ring in flight, half queued for the MMA
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
 };
 
