@@ -46,7 +46,12 @@ struct TcCfg {
     // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
     // MMA run ahead of the arrivals (LAG = STAGES - 1 would lock the two in step)
     static constexpr int LAG = STAGES / 2;
-    static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256;
+    static constexpr size_t TAB_BYTES = TC_MAXCLS * TC_MAXTAPS * 4 + 2 * 256 * 4;  // tap offsets, scale/shift
+    // output staging buffers: two when they fit beside the stage ring, else one
+    static constexpr int EPI_BUFS =
+        (1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256 + TAB_BYTES <= 232448) ? 2 : 1;
+    static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + EPI_BUFS * EPI_BYTES + 256 + TAB_BYTES;
+    static_assert(SMEM <= 232448, "shared memory above the 227 KB per-block limit");
     static constexpr int THREADS = 288;
 };
 
@@ -92,11 +97,16 @@ __global__ void __launch_bounds__(288, 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *epi_smem = base + STAGES * C::STAGE_BYTES;
-    uint64_t *full = (uint64_t *) (epi_smem + 2 * C::EPI_BYTES);
+    uint64_t *full = (uint64_t *) (epi_smem + C::EPI_BUFS * C::EPI_BYTES);
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
     uint64_t *acc_empty = acc_full + 2;
     uint32_t *tmem_holder = (uint32_t *) (acc_empty + 2);
+    // per-class tap offsets (packed y:16 | x:16) and the tile's epilogue scale/shift, in shared
+    // memory: indexing the kernel parameters with runtime values would go through slow generic loads
+    int32_t *tap_tab = (int32_t *) (epi_smem + C::EPI_BUFS * C::EPI_BYTES + 256);
+    float *sc_tab = (float *) (tap_tab + TC_MAXCLS * TC_MAXTAPS);
+    float *sh_tab = sc_tab + 256;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -111,6 +121,10 @@ __global__ void __launch_bounds__(288, 1)
         tc::fence_mbar_init();
         tc::prefetch_tmap(&wmap);
         if (p.epi_tma) tc::prefetch_tmap(&omap);
+    }
+    for (int i = threadIdx.x; i < p.ncls * TC_MAXTAPS; i += blockDim.x) {
+        const int c = i / TC_MAXTAPS, t = i % TC_MAXTAPS;
+        tap_tab[i] = ((int32_t) p.cls[c].toy[t] << 16) | ((int32_t) p.cls[c].tox[t] & 0xFFFF);
     }
     if (warp == 8) {
         tc::tmem_alloc(tmem_holder, 2 * BN);
@@ -130,7 +144,8 @@ __global__ void __launch_bounds__(288, 1)
         uint32_t it = 0;
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
             const Tile tl = decode_tile(p, tile);
-            const TcClass &cl = p.cls[tl.cls];
+            const TcClass cl = p.cls[tl.cls];   // one copy per tile, kept in registers
+            const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
             const int M = p.B * cl.Hg * cl.Wg;
             int rb[8], ry[8], rx[8];
 #pragma unroll
@@ -157,7 +172,8 @@ __global__ void __launch_bounds__(288, 1)
                 uint32_t tap, ci;
                 p.dcin.divmod(k, tap, ci);
                 const bool kval = (int) tap < cl.ntaps;
-                const int oy = kval ? cl.toy[tap] : 0, ox = kval ? cl.tox[tap] : 0;
+                const int32_t to = kval ? taps[tap] : 0;
+                const int oy = to >> 16, ox = (int32_t) (int16_t) (to & 0xFFFF);
                 const uint32_t sA = tc::smem_u32(base + s * C::STAGE_BYTES);
 #pragma unroll
                 for (int i = 0; i < 8; i++) {
@@ -194,9 +210,18 @@ __global__ void __launch_bounds__(288, 1)
         int ebuf = 0;                     // staging buffer toggle
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
             const Tile tl = decode_tile(p, tile);
-            const TcClass &cl = p.cls[tl.cls];
+            const TcClass cl = p.cls[tl.cls];
             const int M = p.B * cl.Hg * cl.Wg;
             const int buf = lt & 1;
+            // this tile's scale/shift into shared memory (the previous tile's readers are done:
+            // they passed the staging barriers, or read them before the arrive below)
+            epi_bar();
+            for (int j = et; j < BN; j += 128) {
+                const int n = min(tl.n0 + j, p.Cout - 1);
+                sc_tab[j] = p.scale ? __ldg(p.scale + n) : 1.0f;
+                sh_tab[j] = p.shift ? __ldg(p.shift + n) : 0.0f;
+            }
+            epi_bar();
             ok = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 3);
             if (!ok) break;
             tc::tc_fence_after();
@@ -225,17 +250,10 @@ __global__ void __launch_bounds__(288, 1)
                 uint32_t pk[32];
 #pragma unroll
                 for (int jj = 0; jj < 32; jj++) {
-                    const int n0 = min(nb + 2 * jj, p.Cout - 1), n1 = min(nb + 2 * jj + 1, p.Cout - 1);
                     float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
                     float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
-                    if (p.scale) {
-                        a *= __ldg(p.scale + n0);
-                        b *= __ldg(p.scale + n1);
-                    }
-                    if (p.shift) {
-                        a += __ldg(p.shift + n0);
-                        b += __ldg(p.shift + n1);
-                    }
+                    a = fmaf(a, sc_tab[c0 + 2 * jj], sh_tab[c0 + 2 * jj]);
+                    b = fmaf(b, sc_tab[c0 + 2 * jj + 1], sh_tab[c0 + 2 * jj + 1]);
                     if (p.relu) {
                         a = fmaxf(a, 0.0f);
                         b = fmaxf(b, 0.0f);
@@ -244,7 +262,10 @@ __global__ void __launch_bounds__(288, 1)
                 }
                 if (p.epi_tma) {
                     // 128 x 64 chunk through shared memory, stored by TMA (out-of-range rows/columns clipped)
-                    if (et == 0) bulk_wait_read<1>();
+                    if (et == 0) {
+                        if (C::EPI_BUFS == 2) bulk_wait_read<1>();
+                        else bulk_wait_read<0>();
+                    }
                     epi_bar();
                     uint8_t *stg = epi_smem + ebuf * C::EPI_BYTES;
 #pragma unroll
@@ -258,7 +279,7 @@ __global__ void __launch_bounds__(288, 1)
                         tma_store_2d(&omap, tc::smem_u32(stg), nb, tl.m0);
                         bulk_commit();
                     }
-                    ebuf ^= 1;
+                    if (C::EPI_BUFS == 2) ebuf ^= 1;
                 } else if (orow && nb < p.Cout) {
                     if (nb + 64 <= p.Cout) {
                         uint4 *dst = reinterpret_cast<uint4 *>(orow + nb);
@@ -283,7 +304,7 @@ __global__ void __launch_bounds__(288, 1)
             uint32_t it = 0, lt = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
                 const Tile tl = decode_tile(p, tile);
-                const int KT = p.cls[tl.cls].ktiles;
+                const int KT = p.cls[tl.cls].ktiles;   // one load per tile
                 const int buf = lt & 1;
                 if (lt >= 2) {
                     ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) - 1) & 1, p.err, 4);

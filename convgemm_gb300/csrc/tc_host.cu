@@ -389,7 +389,7 @@ WgPlan plan_wgrad(const cg_shape &s) {
     w.nchunks = (int) ((g.P + 63) / 64);
     const int base = w.mtiles * w.ntiles;
     const int per_sm = w.bn == 256 ? 1 : 2;
-    int splits = (152 * per_sm + base - 1) / base;
+    int splits = tc_num_sms() * per_sm / base;   // one wave: no partial second wave
     const int max_splits = (w.nchunks + 7) / 8;  // at least 8 chunks (512 pixels) per split
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;

@@ -203,31 +203,51 @@ __global__ void __launch_bounds__(160, 1)
 
 // dW = sum over splits in increasing order, written in the requested layout:
 //   layout 0 (NHWC API): [ci][kh][kw][co];  layout 1 (NCHW API): [co][ci][kh][kw].
+// 32 x 32 tiles of (co, n = tap*Cp + ci): the split partials are read along their
+// contiguous dimension, summed z = 0, 1, ... in order, and written through shared memory.
 __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restrict__ dw, int splits, int xa, int Nx,
-                                    int kn, int C, int Cp, int kh, int kw, int layout) {
-    const long long total = (long long) C * kh * kw * kn;
-    const long long plane = (long long) Nx * kn;
-    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
-         i += (long long) gridDim.x * blockDim.x) {
-        int co, ci, kx, ky;
-        if (layout == 0) {
-            co = (int) (i % kn);
-            long long k = i / kn;
-            ky = (int) (k % kw);
-            kx = (int) ((k / kw) % kh);
-            ci = (int) (k / ((long long) kw * kh));
-        } else {
-            long long k = i % ((long long) C * kh * kw);
-            co = (int) (i / ((long long) C * kh * kw));
-            ky = (int) (k % kw);
-            kx = (int) ((k / kw) % kh);
-            ci = (int) (k / ((long long) kw * kh));
+                                    int kn, int C, int Cp, int khw, int layout) {
+    __shared__ float tile[32][33];
+    const int co0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const size_t plane = (size_t) Nx * kn;
+    for (int k = 0; k < 4; k++) {
+        const int r = ty + 8 * k;
+        int co, n;
+        size_t off;
+        if (xa) {  // partials [n][co]: read along co
+            n = n0 + r;
+            co = co0 + tx;
+            off = (size_t) n * kn + co;
+        } else {   // partials [co][n]: read along n
+            co = co0 + r;
+            n = n0 + tx;
+            off = (size_t) co * Nx + n;
         }
-        const long long n = (long long) (kx * kw + ky) * Cp + ci;
-        const long long off = xa ? n * kn + co : (long long) co * Nx + n;
-        float s = ws[off];
-        for (int z = 1; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
-        dw[i] = s;
+        float s = 0.0f;
+        if (co < kn && n < Nx) {
+            s = ws[off];
+            for (int z = 1; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
+        }
+        if (xa) tile[tx][r] = s;   // tile[co][n]
+        else tile[r][tx] = s;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; k++) {
+        const int r = ty + 8 * k;
+        int co, n;
+        if (layout == 0) {  // write along co
+            co = co0 + tx;
+            n = n0 + r;
+        } else {            // write along n
+            co = co0 + r;
+            n = n0 + tx;
+        }
+        if (co >= kn || n >= Nx) continue;
+        const int tap = n / Cp, ci = n - tap * Cp;
+        if (ci >= C) continue;
+        const size_t o = layout == 0 ? ((size_t) ci * khw + tap) * kn + co : ((size_t) co * C + ci) * khw + tap;
+        dw[o] = layout == 0 ? tile[tx][r] : tile[r][tx];
     }
 }
 
@@ -267,9 +287,7 @@ cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, in
 
 cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
                             int kw, int layout, cudaStream_t st) {
-    const long long total = (long long) C * kh * kw * kn;
-    long long g = (total + 255) / 256;
-    if (g > 152 * 16) g = 152 * 16;
-    wgrad_reduce_kernel<<<(int) g, 256, 0, st>>>(ws, dw, splits, xa, Nx, kn, C, Cp, kh, kw, layout);
+    dim3 grid((kn + 31) / 32, (Nx + 31) / 32), block(32, 8);
+    wgrad_reduce_kernel<<<grid, block, 0, st>>>(ws, dw, splits, xa, Nx, kn, C, Cp, kh * kw, layout);
     return cudaGetLastError();
 }
