@@ -89,10 +89,10 @@ __device__ __forceinline__ Tile decode_tile(const TcConvParams &p, int t) {
     return tl;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool IM2C>
 __global__ void __launch_bounds__(288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
-                   const __grid_constant__ CUtensorMap omap) {
+                   const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
     using C = TcCfg<BN, STAGES>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(288, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            tc::mbar_init(&full[s], 128 + 1);
+            // im2col: the one expect_tx arrival; gather: 128 producer threads + the expect_tx
+            tc::mbar_init(&full[s], IM2C ? 1 : 128 + 1);
             tc::mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; b++) {
@@ -121,6 +122,8 @@ __global__ void __launch_bounds__(288, 1)
         tc::fence_mbar_init();
         tc::prefetch_tmap(&wmap);
         if (p.epi_tma) tc::prefetch_tmap(&omap);
+        if (IM2C)
+            for (int c = 0; c < p.ncls; c++) tc::prefetch_tmap(&amaps.a[c]);
     }
     for (int i = threadIdx.x; i < p.ncls * TC_MAXTAPS; i += blockDim.x) {
         const int c = i / TC_MAXTAPS, t = i % TC_MAXTAPS;
@@ -136,7 +139,36 @@ __global__ void __launch_bounds__(288, 1)
     const uint32_t tmem = *tmem_holder;
     bool ok = true;
 
-    if (warp < 4) {
+    if (IM2C && warp < 4) {
+        // ------------------------------------------------ producer: one thread, im2col TMA for A, TMA for B
+        if (threadIdx.x == 0) {
+            uint32_t it = 0;
+            for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
+                const Tile tl = decode_tile(p, tile);
+                const TcClass &cl = p.cls[tl.cls];
+                const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
+                const int ktiles = cl.ktiles, kbeg = cl.kbeg, mint_y = cl.mint_y, mint_x = cl.mint_x;
+                uint32_t q, jw, j, b;
+                cl.dwg.divmod(tl.m0, q, jw);
+                cl.dhg.divmod(q, b, j);
+                const int h0 = (int) j * cl.isy + cl.lo_y, w0 = (int) jw * cl.isx + cl.lo_x;
+                const CUtensorMap *am = &amaps.a[tl.cls];
+                for (int kt = 0; kt < ktiles; kt++, it++) {
+                    const int s = it % STAGES;
+                    const uint32_t ph = (it / STAGES) & 1;
+                    if (it >= (uint32_t) STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1))) break;
+                    const int tap = kt / p.cpb, ci0 = (kt - tap * p.cpb) * 64;
+                    const int32_t to = taps[tap];
+                    const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
+                    const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
+                    const uint32_t sa = tc::smem_u32(base + s * C::STAGE_BYTES);
+                    tc::mbar_arrive_expect_tx(&full[s], C::A_BYTES + C::B_BYTES);
+                    tc::tma_load_im2col_4d(sa, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
+                    tc::tma_load_2d(sa + C::A_BYTES, &wmap, kbeg + kt * C::BK, tl.n0, &full[s]);
+                }
+            }
+        }
+    } else if (warp < 4) {
         // ------------------------------------------------ producers: gather A, TMA B
         const int t = threadIdx.x;
         const int piece = t & 7;   // 16-byte piece of the 128-byte K row
@@ -342,29 +374,35 @@ __global__ void __launch_bounds__(288, 1)
     if (warp == 8) tc::tmem_dealloc(tmem, 2 * BN);
 }
 
-template <int BN, int STAGES>
-cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
-                      cudaStream_t st) {
+template <int BN, int STAGES, bool IM2C>
+cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
+                      int grid, cudaStream_t st) {
     using C = TcCfg<BN, STAGES>;
-    auto kern = tc_conv_kernel<BN, STAGES>;
+    auto kern = tc_conv_kernel<BN, STAGES, IM2C>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap);
+    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap, amaps);
     return cudaGetLastError();
+}
+
+template <bool IM2C>
+cudaError_t launch_any(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
+                       int grid, cudaStream_t st) {
+    switch (p.bn) {
+        case 64: return launch_bn<64, 8, IM2C>(p, wmap, omap, amaps, grid, st);
+        case 128: return launch_bn<128, 6, IM2C>(p, wmap, omap, amaps, grid, st);
+        case 256: return launch_bn<256, 4, IM2C>(p, wmap, omap, amaps, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace
 
-cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
-                           cudaStream_t st) {
-    switch (p.bn) {
-        case 64: return launch_bn<64, 8>(p, wmap, omap, grid, st);
-        case 128: return launch_bn<128, 6>(p, wmap, omap, grid, st);
-        case 256: return launch_bn<256, 4>(p, wmap, omap, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
+                           const TcMaps &amaps, int grid, cudaStream_t st) {
+    return p.im2col ? launch_any<true>(p, wmap, omap, amaps, grid, st) : launch_any<false>(p, wmap, omap, amaps, grid, st);
 }

@@ -21,6 +21,9 @@ struct TcClass {
     int ktiles;  // K / 64
     int mtiles;  // ceil(B*Hg*Wg / 128)
     int tile0;   // index of the class's first tile in the launch (classes' tiles are concatenated)
+    // im2col-mode TMA: first pixel of row j sits at (j*isy + lo_y, jw*isx + lo_x) in the gathered
+    // tensor and tap t is the unsigned offset (toy[t] - mint_y, tox[t] - mint_x)
+    int lo_y, lo_x, mint_y, mint_x;
     FastDiv dwg, dhg;
     int16_t toy[TC_MAXTAPS], tox[TC_MAXTAPS];
 };
@@ -38,10 +41,18 @@ struct TcConvParams {
     int ntiles;                // tiles along the output channels
     int ntiles_total;          // all tiles of all classes; tile t of a class: m = t / ntiles, n = t % ntiles
     int epi_tma;               // output pixels are the GEMM rows in order: stage in SMEM, TMA store
+    int im2col;                // A loaded by im2col-mode TMA (Cin % 64 == 0), else gathered by cp.async
+    int cpb;                   // 64-channel chunks per tap (Cin / 64) on the im2col path
     int ncls;
     TcClass cls[TC_MAXCLS];
 };
 
+constexpr int TC_MAXIM2COL = 4;  // classes that can use im2col-mode TMA in one launch
+
+struct TcMaps {
+    CUtensorMap a[TC_MAXIM2COL];  // im2col maps of the gathered tensor, one per class
+};
+
 // wmap: packed weights [Cout][K] (box 64 x bn); omap: output [pixels][Cout] (box 64 x 128), used when epi_tma.
-cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, int grid,
-                           cudaStream_t st);
+cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
+                           const TcMaps &amaps, int grid, cudaStream_t st);

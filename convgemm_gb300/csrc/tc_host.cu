@@ -34,7 +34,72 @@ EncodeTiledFn encode_fn() {
 
 int pick_bn(int cout) { return cout >= 256 ? 256 : (cout > 64 ? 128 : 64); }
 
+typedef CUresult (*EncodeIm2colFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const int *, const int *, cuuint32_t, cuuint32_t,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeIm2colFn encode_im2col_fn() {
+    static EncodeIm2colFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeIm2col", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeIm2colFn) p;
+    });
+    return fn;
+}
+
 }  // namespace
+
+// im2col-mode map of a BF16 NHWC tensor [B][H][W][C]: `pixels` pixels x 64 channels per load,
+// bounding box [lo, dim-1+up] per spatial dimension, traversal strides (sh, sw), 128-byte swizzle.
+convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
+                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels) {
+    EncodeIm2colFn fn = encode_im2col_fn();
+    if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col is unavailable");
+    if (((uintptr_t) ptr & 15) || (C * 2) % 16)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "im2col operand not 16-byte aligned");
+    cuuint64_t dims[4] = {(cuuint64_t) C, (cuuint64_t) W, (cuuint64_t) H, (cuuint64_t) B};
+    cuuint64_t strides[3] = {(cuuint64_t) C * 2, (cuuint64_t) W * C * 2, (cuuint64_t) H * W * C * 2};
+    int lower[2] = {lo_w, lo_h};
+    int upper[2] = {up_w, up_h};
+    cuuint32_t estr[4] = {1, (cuuint32_t) sw, (cuuint32_t) sh, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, lower, upper, 64,
+                    (cuuint32_t) pixels, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col failed (%d)", (int) r);
+    return CONVGEMM_SUCCESS;
+}
+
+// Fills the im2col fields of the plan's classes; false when some class cannot use
+// im2col-mode TMA (channels not a multiple of 64, too many classes, corners beyond +-128).
+bool tc_plan_im2col(TcPlan &pl) {
+    if (pl.Cin % 64 || pl.ncls > TC_MAXIM2COL || pl.ncls < 1) return false;
+    for (int c = 0; c < pl.ncls; c++) {
+        TcClass &cl = pl.cls[c];
+        int my = 1 << 30, mx = 1 << 30, Xy = -(1 << 30), Xx = -(1 << 30);
+        for (int t = 0; t < cl.ntaps; t++) {
+            my = cl.toy[t] < my ? cl.toy[t] : my;
+            mx = cl.tox[t] < mx ? cl.tox[t] : mx;
+            Xy = cl.toy[t] > Xy ? cl.toy[t] : Xy;
+            Xx = cl.tox[t] > Xx ? cl.tox[t] : Xx;
+        }
+        cl.mint_y = my;
+        cl.mint_x = mx;
+        cl.lo_y = cl.iby + my;
+        cl.lo_x = cl.ibx + mx;
+        const int up_y = cl.lo_y + (cl.Hg - 1) * cl.isy - (pl.Hin - 1);
+        const int up_x = cl.lo_x + (cl.Wg - 1) * cl.isx - (pl.Win - 1);
+        if (cl.lo_y < -128 || cl.lo_y > 127 || cl.lo_x < -128 || cl.lo_x > 127 || up_y < -128 || up_y > 127 ||
+            up_x < -128 || up_x > 127 || Xy - my > 65535 || Xx - mx > 65535 || cl.isy > 8 || cl.isx > 8)
+            return false;
+    }
+    return true;
+}
 
 // 2-D row-major [rows][cols] tensor, box {64 (cols), box_rows}, 128-byte swizzle.
 convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
@@ -237,15 +302,30 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
     p.ntiles = (pl.Cout + p.bn - 1) / p.bn;
     p.ncls = pl.ncls;
+    TcPlan pi = pl;
+    TcMaps amaps;
+    memset(&amaps, 0, sizeof(amaps));
+    p.im2col = tc_plan_im2col(pi);
+    if (p.im2col) {
+        p.cpb = pl.Cin / 64;
+        for (int c = 0; c < pi.ncls; c++) {
+            const TcClass &cl = pi.cls[c];
+            const int up_y = cl.lo_y + (cl.Hg - 1) * cl.isy - (pl.Hin - 1);
+            const int up_x = cl.lo_x + (cl.Wg - 1) * cl.isx - (pl.Win - 1);
+            if (convgemm_status_t e = tc_make_im2col_map(&amaps.a[c], in, s.b, pl.Hin, pl.Win, pl.Cin, cl.lo_y,
+                                                         cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128))
+                return e;
+        }
+    }
     int t0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
-        p.cls[c] = pl.cls[c];
+        p.cls[c] = pi.cls[c];
         p.cls[c].tile0 = t0;
         t0 += pl.cls[c].mtiles * p.ntiles;
     }
     p.ntiles_total = t0;
     const int grid = t0 < sms ? t0 : sms;
-    return cg_cuda_check(tc_conv_launch(p, wmap, omap, grid, st), "tensor-core conv launch");
+    return cg_cuda_check(tc_conv_launch(p, wmap, omap, amaps, grid, st), "tensor-core conv launch");
 }
 
 // ------------------------------------------------------------ public API

@@ -90,6 +90,17 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         "l"((uint64_t) map), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
+// im2col-mode load of a 4-D NHWC tensor: pixelsPerColumn pixels starting at
+// (w, h, n) inside the map's bounding box, channelsPerPixel channels from c,
+// each pixel displaced by the filter offset (ow, oh); outside the tensor -> 0.
+__device__ __forceinline__ void tma_load_im2col_4d(uint32_t dst, const CUtensorMap *map, int c, int w, int h, int n,
+                                                   uint16_t ow, uint16_t oh, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.im2col.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6], {%7, %8};" ::"r"(dst),
+        "l"((uint64_t) map), "r"(c), "r"(w), "r"(h), "r"(n), "r"(smem_u32(bar)), "h"(ow), "h"(oh)
+        : "memory");
+}
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t) map) : "memory");
 }
