@@ -529,9 +529,20 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.dho = FastDiv(g.ho);
     p.err = cg_device_error_word();
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
+    CUtensorMap xmap;
+    memset(&xmap, 0, sizeof(xmap));
+    {
+        const int up_h = -s.vpad + (g.ho - 1) * s.vstride - (s.h - 1), up_w = -s.hpad + (g.wo - 1) * s.hstride - (s.w - 1);
+        p.im2col = (p.Cp % 64) == 0 && s.vpad <= 128 && s.hpad <= 128 && up_h >= -128 && up_h <= 127 && up_w >= -128 &&
+                   up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
+        if (p.im2col)
+            if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
+                                                         s.vstride, s.hstride, 64))
+                return e;
+    }
     cudaStream_t st = (cudaStream_t) stream;
     if (convgemm_status_t e = cg_cuda_check(
-            tc_wgrad_launch(p, map, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
+            tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
         return e;
     return cg_cuda_check(tc_wgrad_reduce((const float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
                                          s.kw, layout == CONVGEMM_NCHW, st),

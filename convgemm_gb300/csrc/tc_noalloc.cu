@@ -139,9 +139,20 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
     p.dwo = FastDiv(g.wo);
     p.dho = FastDiv(g.ho);
     p.err = d->err;
+    CUtensorMap xmap;
+    memset(&xmap, 0, sizeof(xmap));
+    {
+        const int up_h = -s.vpad + (g.ho - 1) * s.vstride - (s.h - 1), up_w = -s.hpad + (g.wo - 1) * s.hstride - (s.w - 1);
+        p.im2col = (p.Cp % 64) == 0 && s.vpad <= 128 && s.hpad <= 128 && up_h >= -128 && up_h <= 127 && up_w >= -128 &&
+                   up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
+        if (p.im2col)
+            if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
+                                                         s.vstride, s.hstride, 64))
+                return e;
+    }
     cudaStream_t st = (cudaStream_t) stream;
     if (convgemm_status_t e =
-            cg_cuda_check(tc_wgrad_launch(p, map, bn, xa, mtiles, ntiles, splits, st), "weight-gradient launch"))
+            cg_cuda_check(tc_wgrad_launch(p, map, xmap, bn, xa, mtiles, ntiles, splits, st), "weight-gradient launch"))
         return e;
     return cg_cuda_check(
         tc_wgrad_reduce(d->scratch, dw, splits, xa, Nx, s.kn, s.c, Cp, s.kh, s.kw, layout == CONVGEMM_NCHW, st),

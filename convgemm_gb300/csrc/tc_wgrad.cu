@@ -37,9 +37,10 @@ struct WgCfg {
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
 };
 
-template <int BN, int STAGES, bool XA>
+template <int BN, int STAGES, bool XA, bool IM2C>
 __global__ void __launch_bounds__(160, 1)
-    tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap) {
+    tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
+                    const __grid_constant__ CUtensorMap xmap) {
     using C = WgCfg<BN, STAGES, XA>;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
@@ -51,12 +52,13 @@ __global__ void __launch_bounds__(160, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            tc::mbar_init(&full[s], 128 + 1);
+            tc::mbar_init(&full[s], IM2C ? 1 : 128 + 1);
             tc::mbar_init(&empty[s], 1);
         }
         tc::mbar_init(accum, 1);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&dymap);
+        if (IM2C) tc::prefetch_tmap(&xmap);
     }
     if (warp == 4) {
         tc::tmem_alloc(tmem_holder, BN);
@@ -75,7 +77,45 @@ __global__ void __launch_bounds__(160, 1)
     const int KT = min(p.chunks_per_split, p.nchunks - chunk0);
     bool ok = true;
 
-    if (warp < 4) {
+    if (IM2C && warp < 4) {
+        // one thread: im2col TMA for each 64-channel X atom (a fixed tap and channel chunk
+        // for the CTA, 64 consecutive pixels per stage) and tiled TMA for dY
+        if (threadIdx.x == 0) {
+            int a_ci[C::X_ATOMS];
+            uint16_t a_oy[C::X_ATOMS], a_ox[C::X_ATOMS];
+#pragma unroll
+            for (int a = 0; a < C::X_ATOMS; a++) {
+                const int n = min(x0 + 64 * a, p.Nx - 64);  // atoms past Nx load a valid (unused) chunk
+                uint32_t tap, ci;
+                p.dcp.divmod(n, tap, ci);
+                a_ci[a] = ci;
+                a_oy[a] = (uint16_t) (((int) tap / p.kw) * p.vdil);
+                a_ox[a] = (uint16_t) (((int) tap % p.kw) * p.hdil);
+            }
+            const uint32_t xoff = XA ? 0 : C::A_BYTES;
+            const uint32_t dyoff = XA ? C::A_BYTES : 0;
+            for (int kt = 0; kt < KT; kt++) {
+                const int s = kt % STAGES;
+                const uint32_t ph = (kt / STAGES) & 1;
+                if (kt >= STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11))) break;
+                const int pbase = (chunk0 + kt) * C::BK;
+                uint32_t q, ow, oh, b;
+                p.dwo.divmod(pbase, q, ow);
+                p.dho.divmod(q, b, oh);
+                const int h0 = (int) oh * p.vstr - p.vpad, w0 = (int) ow * p.hstr - p.hpad;
+                const uint32_t st0 = tc::smem_u32(base + s * C::STAGE_BYTES);
+                tc::mbar_arrive_expect_tx(&full[s], C::X_ATOMS * 8192 + C::DY_BYTES);
+#pragma unroll
+                for (int a = 0; a < C::X_ATOMS; a++)
+                    tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a], a_oy[a],
+                                           &full[s]);
+#pragma unroll
+                for (int a = 0; a < C::DY_ATOMS; a++)
+                    tc::tma_load_2d(st0 + dyoff + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
+            }
+        }
+        // epilogue below runs on all four warps
+    } else if (warp < 4) {
         const int t = threadIdx.x;
         const int piece = t & 7;
         const int r0 = t >> 3;  // pixel rows r0 + 16*i, i < 4
@@ -140,7 +180,8 @@ __global__ void __launch_bounds__(160, 1)
         tc::fence_proxy_async_smem();
         if (ok)
             for (int kt = (KT > C::LAG ? KT - C::LAG : 0); kt < KT; kt++) tc::mbar_arrive(&full[kt % STAGES]);
-
+    }
+    if (warp < 4) {
         // epilogue: FP32 partial tile -> workspace [split][Mext][Next]
         if (ok) ok = tc::mbar_wait(accum, 0, p.err, 13);
         tc::tc_fence_after();
@@ -251,38 +292,46 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <int BN, int STAGES, bool XA>
-cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, dim3 grid, cudaStream_t st) {
+template <int BN, int STAGES, bool XA, bool IM2C>
+cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUtensorMap &xmap, dim3 grid,
+                      cudaStream_t st) {
     using C = WgCfg<BN, STAGES, XA>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, 160, C::SMEM, st>>>(p, map);
+    kern<<<grid, 160, C::SMEM, st>>>(p, map, xmap);
     return cudaGetLastError();
 }
 
-}  // namespace
-
-cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, int bn, int xa, int mtiles, int ntiles,
-                            int splits, cudaStream_t st) {
-    dim3 grid(mtiles, ntiles, splits);
+template <bool IM2C>
+cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
+                          dim3 grid, cudaStream_t st) {
     if (xa) {
         switch (bn) {
-            case 64: return launch_wg<64, 4, true>(p, dymap, grid, st);
-            case 128: return launch_wg<128, 3, true>(p, dymap, grid, st);
+            case 64: return launch_wg<64, 4, true, IM2C>(p, dymap, xmap, grid, st);
+            case 128: return launch_wg<128, 3, true, IM2C>(p, dymap, xmap, grid, st);
             default: return cudaErrorInvalidValue;
         }
     }
     switch (bn) {
-        case 64: return launch_wg<64, 4, false>(p, dymap, grid, st);
-        case 128: return launch_wg<128, 3, false>(p, dymap, grid, st);
-        case 256: return launch_wg<256, 4, false>(p, dymap, grid, st);
+        case 64: return launch_wg<64, 4, false, IM2C>(p, dymap, xmap, grid, st);
+        case 128: return launch_wg<128, 3, false, IM2C>(p, dymap, xmap, grid, st);
+        case 256: return launch_wg<256, 4, false, IM2C>(p, dymap, xmap, grid, st);
         default: return cudaErrorInvalidValue;
     }
+}
+
+}  // namespace
+
+cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
+                            int mtiles, int ntiles, int splits, cudaStream_t st) {
+    dim3 grid(mtiles, ntiles, splits);
+    return p.im2col ? launch_wg_any<true>(p, dymap, xmap, bn, xa, grid, st)
+                    : launch_wg_any<false>(p, dymap, xmap, bn, xa, grid, st);
 }
 
 cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,

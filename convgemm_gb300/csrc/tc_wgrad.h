@@ -13,9 +13,11 @@ struct TcWgradParams {
     int nchunks, chunks_per_split;  // 64-pixel chunks of the reduction, per split
     FastDiv dcp, dwo, dho;
     int *err;
+    int im2col;               // X by im2col-mode TMA (Cp % 64 == 0), else by cp.async gathers
 };
 
-cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, int bn, int xa, int mtiles, int ntiles,
-                            int splits, cudaStream_t st);
+// xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
+cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
+                            int mtiles, int ntiles, int splits, cudaStream_t st);
 cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
                             int kw, int layout, cudaStream_t st);
