@@ -46,7 +46,8 @@ struct TcCfg {
     // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
     // MMA run ahead of the arrivals (LAG = STAGES - 1 would lock the two in step)
     static constexpr int LAG = STAGES / 2;
-    static constexpr size_t TAB_BYTES = TC_MAXCLS * TC_MAXTAPS * 4 + 2 * 256 * 4;  // tap offsets, scale/shift
+    // shared tables: tap offsets, the class table, scale/shift (whole vectors up to 1024 channels)
+    static constexpr size_t TAB_BYTES = TC_MAXCLS * TC_MAXTAPS * 4 + TC_MAXCLS * 128 + 2 * 1024 * 4;
     // output staging buffers: two when they fit beside the stage ring, else one
     static constexpr int EPI_BUFS =
         (1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256 + TAB_BYTES <= 232448) ? 2 : 1;
@@ -78,14 +79,23 @@ struct Tile {
     int cls, m0, n0;
 };
 
-__device__ __forceinline__ Tile decode_tile(const TcConvParams &p, int t) {
+// The scalars of a class, copied to shared memory at kernel start (reading the
+// kernel parameters with a runtime class index would cost generic-memory loads
+// on every tile).
+struct ClsS {
+    int Hg, Wg, oy0, ox0, osy, osx, isy, isx, iby, ibx, ntaps, kbeg, ktiles, tile0, lo_y, lo_x, mint_y, mint_x;
+    FastDiv dwg, dhg;
+};
+static_assert(sizeof(ClsS) <= 128, "class table entry");
+
+__device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntiles, int bn, int t) {
     int c = 0;
-    while (c + 1 < p.ncls && t >= p.cls[c + 1].tile0) c++;
-    const int local = t - p.cls[c].tile0;
+    while (c + 1 < ncls && t >= cls[c + 1].tile0) c++;
+    const int local = t - cls[c].tile0;
     Tile tl;
     tl.cls = c;
-    tl.m0 = (local / p.ntiles) * 128;
-    tl.n0 = (local % p.ntiles) * p.bn;
+    tl.m0 = (local / ntiles) * 128;
+    tl.n0 = (local % ntiles) * bn;
     return tl;
 }
 
@@ -105,8 +115,10 @@ __global__ void __launch_bounds__(288, 1)
     // per-class tap offsets (packed y:16 | x:16) and the tile's epilogue scale/shift, in shared
     // memory: indexing the kernel parameters with runtime values would go through slow generic loads
     int32_t *tap_tab = (int32_t *) (epi_smem + C::EPI_BUFS * C::EPI_BYTES + 256);
-    float *sc_tab = (float *) (tap_tab + TC_MAXCLS * TC_MAXTAPS);
-    float *sh_tab = sc_tab + 256;
+    ClsS *cls_tab = (ClsS *) (tap_tab + TC_MAXCLS * TC_MAXTAPS);
+    float *sc_tab = (float *) (cls_tab + TC_MAXCLS);   // [1024]: all channels, or the tile's BN
+    float *sh_tab = sc_tab + 1024;
+    const bool sc_all = p.Cout <= 1024;              // whole scale/shift vectors fit
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -129,6 +141,19 @@ __global__ void __launch_bounds__(288, 1)
         const int c = i / TC_MAXTAPS, t = i % TC_MAXTAPS;
         tap_tab[i] = ((int32_t) p.cls[c].toy[t] << 16) | ((int32_t) p.cls[c].tox[t] & 0xFFFF);
     }
+    if (threadIdx.x < (unsigned) p.ncls) {
+        const TcClass &c = p.cls[threadIdx.x];
+        ClsS &d = cls_tab[threadIdx.x];
+        d.Hg = c.Hg; d.Wg = c.Wg; d.oy0 = c.oy0; d.ox0 = c.ox0; d.osy = c.osy; d.osx = c.osx;
+        d.isy = c.isy; d.isx = c.isx; d.iby = c.iby; d.ibx = c.ibx; d.ntaps = c.ntaps; d.kbeg = c.kbeg;
+        d.ktiles = c.ktiles; d.tile0 = c.tile0; d.lo_y = c.lo_y; d.lo_x = c.lo_x; d.mint_y = c.mint_y;
+        d.mint_x = c.mint_x; d.dwg = c.dwg; d.dhg = c.dhg;
+    }
+    if (sc_all)
+        for (int n = threadIdx.x; n < p.Cout; n += blockDim.x) {
+            sc_tab[n] = p.scale ? __ldg(p.scale + n) : 1.0f;
+            sh_tab[n] = p.shift ? __ldg(p.shift + n) : 0.0f;
+        }
     if (warp == 8) {
         tc::tmem_alloc(tmem_holder, 2 * BN);
         tc::tmem_relinquish();
@@ -144,8 +169,8 @@ __global__ void __launch_bounds__(288, 1)
         if (threadIdx.x == 0) {
             uint32_t it = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
-                const Tile tl = decode_tile(p, tile);
-                const TcClass &cl = p.cls[tl.cls];
+                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+                const ClsS &cl = cls_tab[tl.cls];
                 const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
                 const int ktiles = cl.ktiles, kbeg = cl.kbeg, mint_y = cl.mint_y, mint_x = cl.mint_x;
                 uint32_t q, jw, j, b;
@@ -153,11 +178,11 @@ __global__ void __launch_bounds__(288, 1)
                 cl.dhg.divmod(q, b, j);
                 const int h0 = (int) j * cl.isy + cl.lo_y, w0 = (int) jw * cl.isx + cl.lo_x;
                 const CUtensorMap *am = &amaps.a[tl.cls];
+                int tap = 0, ci0 = 0;   // k = tap*Cin + ci0, walked incrementally
                 for (int kt = 0; kt < ktiles; kt++, it++) {
                     const int s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1;
                     if (it >= (uint32_t) STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1))) break;
-                    const int tap = kt / p.cpb, ci0 = (kt - tap * p.cpb) * 64;
                     const int32_t to = taps[tap];
                     const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
                     const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
@@ -165,6 +190,11 @@ __global__ void __launch_bounds__(288, 1)
                     tc::mbar_arrive_expect_tx(&full[s], C::A_BYTES + C::B_BYTES);
                     tc::tma_load_im2col_4d(sa, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
                     tc::tma_load_2d(sa + C::A_BYTES, &wmap, kbeg + kt * C::BK, tl.n0, &full[s]);
+                    ci0 += 64;
+                    if (ci0 == p.Cin) {
+                        ci0 = 0;
+                        tap++;
+                    }
                 }
             }
         }
@@ -175,8 +205,8 @@ __global__ void __launch_bounds__(288, 1)
         const int r0 = t >> 3;     // rows r0 + 16*i
         uint32_t it = 0;
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
-            const Tile tl = decode_tile(p, tile);
-            const TcClass cl = p.cls[tl.cls];   // one copy per tile, kept in registers
+            const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+            const ClsS &cl = cls_tab[tl.cls];
             const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
             const int M = p.B * cl.Hg * cl.Wg;
             int rb[8], ry[8], rx[8];
@@ -241,19 +271,24 @@ __global__ void __launch_bounds__(288, 1)
         uint32_t lt = 0;                  // local tile count
         int ebuf = 0;                     // staging buffer toggle
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
-            const Tile tl = decode_tile(p, tile);
-            const TcClass cl = p.cls[tl.cls];
+            const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+            const ClsS &cl = cls_tab[tl.cls];
             const int M = p.B * cl.Hg * cl.Wg;
             const int buf = lt & 1;
-            // this tile's scale/shift into shared memory (the previous tile's readers are done:
-            // they passed the staging barriers, or read them before the arrive below)
-            epi_bar();
-            for (int j = et; j < BN; j += 128) {
-                const int n = min(tl.n0 + j, p.Cout - 1);
-                sc_tab[j] = p.scale ? __ldg(p.scale + n) : 1.0f;
-                sh_tab[j] = p.shift ? __ldg(p.shift + n) : 0.0f;
+            const float *scp = sc_tab, *shp = sh_tab;
+            if (sc_all) {
+                scp += tl.n0;
+                shp += tl.n0;
+            } else {
+                // this tile's scale/shift (the previous tile's readers passed the barrier below)
+                epi_bar();
+                for (int j = et; j < BN; j += 128) {
+                    const int n = min(tl.n0 + j, p.Cout - 1);
+                    sc_tab[j] = p.scale ? __ldg(p.scale + n) : 1.0f;
+                    sh_tab[j] = p.shift ? __ldg(p.shift + n) : 0.0f;
+                }
+                epi_bar();
             }
-            epi_bar();
             ok = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 3);
             if (!ok) break;
             tc::tc_fence_after();
@@ -284,8 +319,8 @@ __global__ void __launch_bounds__(288, 1)
                 for (int jj = 0; jj < 32; jj++) {
                     float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
                     float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
-                    a = fmaf(a, sc_tab[c0 + 2 * jj], sh_tab[c0 + 2 * jj]);
-                    b = fmaf(b, sc_tab[c0 + 2 * jj + 1], sh_tab[c0 + 2 * jj + 1]);
+                    a = fmaf(a, scp[c0 + 2 * jj], shp[c0 + 2 * jj]);
+                    b = fmaf(b, scp[c0 + 2 * jj + 1], shp[c0 + 2 * jj + 1]);
                     if (p.relu) {
                         a = fmaxf(a, 0.0f);
                         b = fmaxf(b, 0.0f);
@@ -335,8 +370,8 @@ __global__ void __launch_bounds__(288, 1)
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
             uint32_t it = 0, lt = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
-                const Tile tl = decode_tile(p, tile);
-                const int KT = p.cls[tl.cls].ktiles;   // one load per tile
+                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+                const int KT = cls_tab[tl.cls].ktiles;
                 const int buf = lt & 1;
                 if (lt >= 2) {
                     ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) - 1) & 1, p.err, 4);

@@ -50,19 +50,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // Budget of one wait: far above any legitimate in-CTA wait (microseconds).
 constexpr uint64_t WAIT_BUDGET_NS = 2000000000ull;  // 2 s
 
-// Waits for the phase of `parity` to complete.  On timeout it records `code`
-// in *err (first writer wins) and returns false; callers then stop waiting.
+// Waits for the phase of `parity` to complete.  try_wait suspends the thread
+// in hardware until the phase completes or a short time limit passes, so the
+// loop just polls it (a software sleep would wake late and stall the ring);
+// the clock is read every 1024 polls.  On timeout it records `code` in *err
+// (first writer wins) and returns false; callers then stop waiting.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
-    for (int i = 0; i < 256; i++)
+    uint64_t t0 = 0;
+    for (uint32_t i = 1;; i++) {
         if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer();
-    while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (globaltimer() - t0 > WAIT_BUDGET_NS) {
-            if (err) atomicCAS(err, 0, code);
-            return false;
+        if ((i & 1023) == 0) {
+            const uint64_t now = globaltimer();
+            if (t0 == 0) {
+                t0 = now;
+            } else if (now - t0 > WAIT_BUDGET_NS) {
+                if (err) atomicCAS(err, 0, code);
+                return false;
+            }
         }
-        __nanosleep(64);
     }
 }
 
