@@ -214,8 +214,14 @@ class Net:
                 d["dw32"] = torch.empty(s.c * s.kh * s.kw * s.kn, device=dev)
 
     def launches_bf16(self):
-        # fold, pack fwd, fwd, [pack dgrad, dgrad], wgrad, wgrad reduce
-        return sum(5 if d["first"] else 7 for d in self.L)
+        # fold, pack fwd (+ a K-padding fill when kh*kw*c8 is not a multiple of 64), fwd,
+        # [pack dgrad, dgrad], wgrad, wgrad reduce
+        n = 0
+        for d in self.L:
+            s = d["s"]
+            n += 5 if d["first"] else 7
+            n += 1 if (s.kh * s.kw * c8(s.c)) % 64 else 0
+        return n
 
     def launches_f32(self):
         return sum(3 if d["first"] else 4 for d in self.L)

@@ -19,7 +19,34 @@ __device__ __forceinline__ float wref(const float *w, int nchw, int C, int kh, i
     return nchw ? w[(size_t) co * ((size_t) C * kh * kw) + k] : w[k * kn + co];
 }
 
-// out[co][k], k = (kx*kw + ky)*Cp + ci, zero for padded ci and k.
+// out[co][k], k = (kx*kw + ky)*Cp + ci, zero for padded ci and k.  One 32x32 tile of
+// (ci, co) at one tap per block: reads along co (contiguous in the NHWC-API layout),
+// writes along ci (contiguous in the packed row) through shared memory.
+__global__ void pack_fwd_tiled_kernel(const float *__restrict__ w, int C, int khw, int kn, int Cp, int Kpad,
+                                      bf16 *__restrict__ out) {
+    __shared__ float tile[32][33];
+    const int tap = blockIdx.z, ci0 = blockIdx.x * 32, co0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    for (int i = ty; i < 32; i += 8) {
+        const int ci = ci0 + i, co = co0 + tx;
+        tile[i][tx] = (ci < C && co < kn) ? w[((size_t) ci * khw + tap) * kn + co] : 0.0f;
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int co = co0 + j, ci = ci0 + tx;
+        if (co < kn && ci < Cp) out[(size_t) co * Kpad + (size_t) tap * Cp + ci] = __float2bfloat16_rn(tile[tx][j]);
+    }
+}
+
+// zero of the K padding columns [khw*Cp, Kpad) of every row
+__global__ void pack_fwd_tail_kernel(int kn, int Kbeg, int Kpad, bf16 *__restrict__ out) {
+    const int width = Kpad - Kbeg;
+    const long long total = (long long) kn * width;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x)
+        out[(i / width) * Kpad + Kbeg + i % width] = __float2bfloat16_rn(0.0f);
+}
+
 __global__ void pack_fwd_kernel(const float *__restrict__ w, int nchw, int C, int kh, int kw, int kn, int Cp,
                                 int Kpad, bf16 *__restrict__ out) {
     const long long total = (long long) kn * Kpad;
@@ -96,7 +123,17 @@ int grid_for(long long n) {
 
 cudaError_t prep_pack_fwd(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *out,
                           cudaStream_t st) {
-    pack_fwd_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, (bf16 *) out);
+    if (nchw) {
+        pack_fwd_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad,
+                                                                        (bf16 *) out);
+        return cudaGetLastError();
+    }
+    const int khw = kh * kw;
+    dim3 grid((Cp + 31) / 32, (kn + 31) / 32, khw), block(32, 8);
+    pack_fwd_tiled_kernel<<<grid, block, 0, st>>>(w, C, khw, kn, Cp, Kpad, (bf16 *) out);
+    if (Kpad > khw * Cp)
+        pack_fwd_tail_kernel<<<grid_for((long long) kn * (Kpad - khw * Cp)), 256, 0, st>>>(kn, khw * Cp, Kpad,
+                                                                                          (bf16 *) out);
     return cudaGetLastError();
 }
 
