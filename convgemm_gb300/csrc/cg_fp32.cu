@@ -376,8 +376,17 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     const long long total = (long long) K * kn;
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
          i += (long long) gridDim.x * blockDim.x) {
+        // loads eight blocks ahead, adds strictly in block order
         float s = ws[i];
-        for (int z = 1; z < nblocks; z++) s = __fadd_rn(s, ws[(size_t) z * total + i]);
+        int z = 1;
+        for (; z + 8 <= nblocks; z += 8) {
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = ws[(size_t) (z + j) * total + i];
+#pragma unroll
+            for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
+        }
+        for (; z < nblocks; z++) s = __fadd_rn(s, ws[(size_t) z * total + i]);
         const int m = (int) (i / kn), n = (int) (i % kn);
         dw[nchw ? ((size_t) n * K + m) : (size_t) i] = s;
     }

@@ -267,8 +267,17 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
         }
         float s = 0.0f;
         if (co < kn && n < Nx) {
+            // loads eight splits ahead, adds strictly in split order
             s = ws[off];
-            for (int z = 1; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
+            int z = 1;
+            for (; z + 8 <= splits; z += 8) {
+                float v[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) v[j] = ws[(z + j) * plane + off];
+#pragma unroll
+                for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
+            }
+            for (; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
         }
         if (xa) tile[tx][r] = s;   // tile[co][n]
         else tile[r][tx] = s;
