@@ -36,11 +36,16 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-template <int BN, int STAGES>
+// KB 64-deep K blocks per pipeline stage: one full barrier and one MMA commit
+// cover KB blocks (a barrier round trip costs ~400 cycles, a 128 x 64 x 64 block
+// of MMAs ~150).
+template <int BN, int STAGES, int KB = 1>
 struct TcCfg {
     static constexpr int BM = 128, BK = 64;
-    static constexpr uint32_t A_BYTES = BM * BK * 2;
-    static constexpr uint32_t B_BYTES = BN * BK * 2;
+    static constexpr uint32_t A_BLOCK = BM * BK * 2;   // one 64-deep block of A (128 rows x 128 B)
+    static constexpr uint32_t B_BLOCK = BN * BK * 2;
+    static constexpr uint32_t A_BYTES = KB * A_BLOCK;
+    static constexpr uint32_t B_BYTES = KB * B_BLOCK;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t EPI_BYTES = BM * 64 * 2;  // one 128 x 64 BF16 output chunk
     // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
@@ -99,11 +104,12 @@ __device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntile
     return tl;
 }
 
-template <int BN, int STAGES, bool IM2C>
+template <int BN, int STAGES, int KB, bool IM2C>
 __global__ void __launch_bounds__(288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
-    using C = TcCfg<BN, STAGES>;
+    using C = TcCfg<BN, STAGES, KB>;
+    static_assert(IM2C || KB == 1, "the cp.async gather fills one K block per stage");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *epi_smem = base + STAGES * C::STAGE_BYTES;
@@ -179,21 +185,25 @@ __global__ void __launch_bounds__(288, 1)
                 const int h0 = (int) j * cl.isy + cl.lo_y, w0 = (int) jw * cl.isx + cl.lo_x;
                 const CUtensorMap *am = &amaps.a[tl.cls];
                 int tap = 0, ci0 = 0;   // k = tap*Cin + ci0, walked incrementally
-                for (int kt = 0; kt < ktiles; kt++, it++) {
+                for (int kt = 0; kt < ktiles; kt += KB, it++) {
                     const int s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1;
                     if (it >= (uint32_t) STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1))) break;
-                    const int32_t to = taps[tap];
-                    const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
-                    const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
+                    const int nkb = min(KB, ktiles - kt);
                     const uint32_t sa = tc::smem_u32(base + s * C::STAGE_BYTES);
-                    tc::mbar_arrive_expect_tx(&full[s], C::A_BYTES + C::B_BYTES);
-                    tc::tma_load_im2col_4d(sa, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
-                    tc::tma_load_2d(sa + C::A_BYTES, &wmap, kbeg + kt * C::BK, tl.n0, &full[s]);
-                    ci0 += 64;
-                    if (ci0 == p.Cin) {
-                        ci0 = 0;
-                        tap++;
+                    tc::mbar_arrive_expect_tx(&full[s], nkb * (C::A_BLOCK + C::B_BLOCK));
+                    for (int kb = 0; kb < nkb; kb++) {
+                        const int32_t to = taps[tap];
+                        const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
+                        const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
+                        tc::tma_load_im2col_4d(sa + kb * C::A_BLOCK, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
+                        tc::tma_load_2d(sa + C::A_BYTES + kb * C::B_BLOCK, &wmap, kbeg + (kt + kb) * C::BK, tl.n0,
+                                        &full[s]);
+                        ci0 += 64;
+                        if (ci0 == p.Cin) {
+                            ci0 = 0;
+                            tap++;
+                        }
                     }
                 }
             }
@@ -379,7 +389,7 @@ __global__ void __launch_bounds__(288, 1)
                     tc::tc_fence_after();
                 }
                 const uint32_t dt = tmem + (uint32_t) (buf * BN);
-                for (int kt = 0; kt < KT; kt++, it++) {
+                for (int kt = 0; kt < KT; kt += KB, it++) {
                     const int s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1;
                     if (!tc::mbar_wait(&full[s], ph, p.err, 2)) {
@@ -387,13 +397,16 @@ __global__ void __launch_bounds__(288, 1)
                         break;
                     }
                     tc::tc_fence_after();
+                    const int nkb = min(KB, KT - kt);
                     const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
                     const uint32_t b0 = a0 + C::A_BYTES;
+                    for (int kb = 0; kb < nkb; kb++) {
 #pragma unroll
-                    for (int k = 0; k < C::BK / 16; k++) {
-                        const uint64_t ad = tc::sw128_desc(a0 + k * 32, 16, 1024);
-                        const uint64_t bd = tc::sw128_desc(b0 + k * 32, 16, 1024);
-                        tc::mma_f16(dt, ad, bd, idesc, (kt | k) != 0);
+                        for (int k = 0; k < C::BK / 16; k++) {
+                            const uint64_t ad = tc::sw128_desc(a0 + kb * C::A_BLOCK + k * 32, 16, 1024);
+                            const uint64_t bd = tc::sw128_desc(b0 + kb * C::B_BLOCK + k * 32, 16, 1024);
+                            tc::mma_f16(dt, ad, bd, idesc, (kt | kb | k) != 0);
+                        }
                     }
                     tc::mma_commit(&empty[s]);
                 }
@@ -409,11 +422,11 @@ __global__ void __launch_bounds__(288, 1)
     if (warp == 8) tc::tmem_dealloc(tmem, 2 * BN);
 }
 
-template <int BN, int STAGES, bool IM2C>
+template <int BN, int STAGES, int KB, bool IM2C>
 cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
                       int grid, cudaStream_t st) {
-    using C = TcCfg<BN, STAGES>;
-    auto kern = tc_conv_kernel<BN, STAGES, IM2C>;
+    using C = TcCfg<BN, STAGES, KB>;
+    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -424,20 +437,25 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUte
     return cudaGetLastError();
 }
 
-template <bool IM2C>
-cudaError_t launch_any(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
-                       int grid, cudaStream_t st) {
-    switch (p.bn) {
-        case 64: return launch_bn<64, 8, IM2C>(p, wmap, omap, amaps, grid, st);
-        case 128: return launch_bn<128, 6, IM2C>(p, wmap, omap, amaps, grid, st);
-        case 256: return launch_bn<256, 4, IM2C>(p, wmap, omap, amaps, grid, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
 }  // namespace
 
+// Stage shapes (all ~192 KB of ring): im2col path BN=64: 4 stages of 2 K blocks;
+// BN=128: 3 stages of 2 blocks; BN=256: 3 stages of 1 block with two output staging
+// buffers (its tiles are often single-block 1x1 layers bound by the output stores).
 cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
                            const TcMaps &amaps, int grid, cudaStream_t st) {
-    return p.im2col ? launch_any<true>(p, wmap, omap, amaps, grid, st) : launch_any<false>(p, wmap, omap, amaps, grid, st);
+    if (p.im2col) {
+        switch (p.bn) {
+            case 64: return launch_bn<64, 4, 2, true>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 3, 2, true>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 1, true>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    switch (p.bn) {
+        case 64: return launch_bn<64, 8, 1, false>(p, wmap, omap, amaps, grid, st);
+        case 128: return launch_bn<128, 6, 1, false>(p, wmap, omap, amaps, grid, st);
+        case 256: return launch_bn<256, 4, 1, false>(p, wmap, omap, amaps, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
