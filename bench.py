@@ -226,29 +226,41 @@ class Net:
     def launches_f32(self):
         return sum(3 if d["first"] else 4 for d in self.L)
 
-    def step_bf16(self, timers=None):
-        tc = self.tc
+    def step_bf16(self):
+        """One BF16 step: weight preparation, forward, input gradient, weight gradient of every layer."""
+        for fam in ("prep", "fwd", "dgrad", "wgrad"):
+            self.step_family(fam)
+
+    def step_family(self, fam):
+        """Launches one kernel family of the BF16 step; returns how many kernels it launched."""
+        tc, cg = self.tc, self.cg
+        n = 0
         for d in self.L:
             s = d["s"]
-            ev = timers.start("fwd", d) if timers else None
-            tc.fold_epilogue(s.kn, d["scale"], d["shift"], mean=d["mean"], inv_std=d["inv_std"], gamma=d["gamma"],
-                             beta=d["beta"])
-            tc.pack_weights(self.cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
-            if timers:
-                timers.mark(ev, "prep")
-            tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"])
-            if timers:
-                timers.mark(ev, "fwd")
-            if not d["first"]:
-                tc.pack_weights(self.cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
-                if timers:
-                    timers.mark(ev, "prep")
+            if fam == "prep":
+                tc.fold_epilogue(s.kn, d["scale"], d["shift"], mean=d["mean"], inv_std=d["inv_std"],
+                                 gamma=d["gamma"], beta=d["beta"])
+                tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
+                n += 2 + (1 if (s.kh * s.kw * c8(s.c)) % 64 else 0)
+                if not d["first"]:
+                    tc.pack_weights(cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
+                    n += 1
+            elif fam == "fwd":
+                tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"])
+                n += 1
+            elif fam == "dgrad" and not d["first"]:
                 tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"])
-                if timers:
-                    timers.mark(ev, "dgrad")
-            tc.wgrad_bf16(self.cg.NHWC, s, d["dy"], d["x"], d["dw"], self.ws)
-            if timers:
-                timers.mark(ev, "wgrad")
+                n += 1
+            elif fam == "wgrad":
+                tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], self.ws)
+                n += 2
+        return n
+
+    def family_flops(self, fam):
+        if fam == "prep":
+            return 0
+        return sum(conv_flops(self.layers[d["i"]], self.batch) for d in self.L
+                   if not (fam == "dgrad" and d["first"]))
 
     def step_f32(self):
         cg = self.cg
@@ -259,32 +271,6 @@ class Net:
             if not d["first"]:
                 cg.dgrad_f32(cg.NHWC, s, d["w32"], d["dy32"], d["dx32"], accumulate=False)
             cg.wgrad_f32(cg.NHWC, s, d["dy32"], d["x32"], d["dw32"], self.ws32)
-
-
-class KernelTimers:
-    """CUDA events between consecutive launches of one (untimed) step, binned by kernel family."""
-
-    def __init__(self, torch):
-        self.torch = torch
-        self.rec = []
-
-    def start(self, kind, d):
-        e = self.torch.cuda.Event(enable_timing=True)
-        e.record()
-        return {"last": e, "d": d}
-
-    def mark(self, ev, kind):
-        e = self.torch.cuda.Event(enable_timing=True)
-        e.record()
-        self.rec.append((kind, ev["d"], ev["last"], e))
-        ev["last"] = e
-
-    def totals(self):
-        self.torch.cuda.synchronize()
-        out = {}
-        for kind, d, a, b in self.rec:
-            out.setdefault(kind, []).append((d, a.elapsed_time(b)))
-        return out
 
 
 def layer_bytes(l, batch, elem=2):
@@ -428,27 +414,30 @@ def main():
     cg.check_device()
     value = world * batch / (ms / 1000.0)
 
-    # ---- per-kernel-family times of one eager step (untimed), for the roofline
-    timers = KernelTimers(torch)
-    net.step_bf16(timers)
-    fam = timers.totals()
+    # ---- per-kernel-family device times: each family captured as its own graph and replayed
     peaks, peak_kind = read_peaks()
     fam_summary = {}
-    for kind, recs in fam.items():
-        tms = sum(t for _, t in recs)
-        if kind in ("fwd", "dgrad", "wgrad"):
-            fl = sum(conv_flops(layers[d["i"]], batch) for d, _ in recs)
-        else:
-            fl = 0
-        fam_summary[kind] = {"ms": tms, "launches": len(recs), "tflops": (fl / (tms / 1000) / 1e12) if tms else 0}
-    dominant = max((k for k in fam_summary if k != "prep"), key=lambda k: fam_summary[k]["ms"])
+    for fam in ("prep", "fwd", "dgrad", "wgrad"):
+        g_f = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            with torch.cuda.graph(g_f, stream=stream):
+                n_launch = net.step_family(fam)
+        torch.cuda.synchronize()
+        ms_f = timed(torch, g_f.replay, max(5, args.steps), 2, torch.cuda.current_stream())
+        fl = net.family_flops(fam)
+        fam_summary[fam] = {"ms": ms_f, "launches": n_launch, "tflops": fl / (ms_f / 1000) / 1e12 if fl else 0.0,
+                            "gflop": fl / 1e9}
+        del g_f
+    kern_of = {"fwd": "tc_conv_kernel (forward)", "dgrad": "tc_conv_kernel (input gradient)",
+               "wgrad": "tc_wgrad_kernel + wgrad_reduce_kernel"}
+    dominant = max(("fwd", "dgrad", "wgrad"), key=lambda k: fam_summary[k]["ms"])
     dom = fam_summary[dominant]
-    kernel_name = {"fwd": "tc_conv_kernel (forward)", "dgrad": "tc_conv_kernel (input gradient)",
-                   "wgrad": "tc_wgrad_kernel + wgrad_reduce_kernel"}[dominant]
-    roofline = {"bound": "tensor", "kernel": kernel_name, "achieved": dom["tflops"],
+    roofline = {"bound": "tensor", "kernel": kern_of[dominant], "achieved": dom["tflops"],
                 "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
                 "frac": dom["tflops"] / peaks["bf16_tflops_sustained"], "traffic": None,
                 "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
+                "how": "each kernel family of the step captured as its own CUDA graph, replayed, CUDA events; "
+                       "achieved = algorithmic FLOPs (2*b*ho*wo*kn*c*kh*kw per conv) / device time",
                 "families": fam_summary}
 
     if args.per_layer and rank == 0:
