@@ -106,6 +106,15 @@ def lib():
         L.convgemm_wgrad_bf16_workspace_size.restype = ctypes.c_size_t
         L.convgemm_wgrad_bf16.argtypes = [_I, SP, _VP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
         L.convgemm_wgrad_bf16_noalloc.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
+        L.convgemm_fp8_quantize.argtypes = [ctypes.c_size_t, _I, _VP, _VP, _VP, _VP]
+        L.convgemm_fp8_weights_size.argtypes = [SP]
+        L.convgemm_fp8_weights_size.restype = ctypes.c_size_t
+        L.convgemm_fp8_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
+        L.convgemm_fp8_epilogue_scales.argtypes = [_I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]
+        L.convgemm_fwd_fp8.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
+        L.convgemm_split_bf16x2.argtypes = [ctypes.c_size_t, _VP, _VP, _VP, _VP]
+        L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
+        L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         _lib = L
     return _lib
 

@@ -2,6 +2,7 @@
 // K-major operand the tcgen05 kernels load with TMA, the FP64 batch-norm fold,
 // activation casts, and the fixed-order reduction of weight-gradient splits.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include "cg_common.cuh"
 #include "prep.h"
@@ -114,6 +115,94 @@ __global__ void to_bf16_nhwc_kernel(const float *__restrict__ in, int nchw, int 
     }
 }
 
+// ------------------------------------------------------ FP8 and 3xBF16 forms
+constexpr float E4M3_MAX = 448.0f;
+
+__device__ __forceinline__ uint8_t to_e4m3(float v) {
+    return (uint8_t) __nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+}
+
+// amax (as the bit pattern of a non-negative float, so atomicMax on unsigned orders it)
+__global__ void amax_kernel(const void *__restrict__ in, int in_bf16, long long n, unsigned *amax_bits) {
+    float m = 0.0f;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float v = in_bf16 ? __bfloat162float(((const bf16 *) in)[i]) : ((const float *) in)[i];
+        m = fmaxf(m, fabsf(v));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(amax_bits, __float_as_uint(m));
+}
+
+// per-tensor scale = amax / 448 (1 for an all-zero tensor); x_q = e4m3(x / scale)
+__global__ void quant_e4m3_kernel(const void *__restrict__ in, int in_bf16, long long n, const unsigned *amax_bits,
+                                  uint8_t *__restrict__ out, float *scale_out) {
+    const float amax = __uint_as_float(*amax_bits);
+    const float sc = amax > 0.0f ? amax / E4M3_MAX : 1.0f;
+    const float inv = 1.0f / sc;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *scale_out = sc;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float v = in_bf16 ? __bfloat162float(((const bf16 *) in)[i]) : ((const float *) in)[i];
+        out[i] = to_e4m3(v * inv);
+    }
+}
+
+// per-output-channel weight scale (NHWC-API weights [K][kn]: threads along co, loop over K)
+__global__ void wscale_kernel(const float *__restrict__ w, int nchw, int K, int kn, float *wscale) {
+    const int co = blockIdx.x * blockDim.x + threadIdx.x;
+    if (co >= kn) return;
+    float m = 0.0f;
+    for (int k = 0; k < K; k++) m = fmaxf(m, fabsf(nchw ? w[(size_t) co * K + k] : w[(size_t) k * kn + co]));
+    wscale[co] = m > 0.0f ? m / E4M3_MAX : 1.0f;
+}
+
+// E4M3 operand [co][tap*Cp + ci] = w / wscale[co]
+__global__ void pack_fp8_kernel(const float *__restrict__ w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad,
+                                const float *__restrict__ wscale, uint8_t *__restrict__ out) {
+    const long long total = (long long) kn * Kpad;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x) {
+        const int co = (int) (i / Kpad), k = (int) (i % Kpad);
+        const int tap = k / Cp, ci = k % Cp;
+        float v = 0.0f;
+        if (tap < kh * kw && ci < C) v = wref(w, nchw, C, kh, kw, kn, ci, tap / kw, tap % kw, co) / wscale[co];
+        out[i] = to_e4m3(v);
+    }
+}
+
+// scale' = scale * wscale * xscale (the two quantisation scales folded into the epilogue)
+__global__ void fp8_scales_kernel(int kn, const float *scale, const float *shift, const float *wscale,
+                                  const float *xscale, float *out_scale, float *out_shift) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= kn) return;
+    out_scale[n] = (scale ? scale[n] : 1.0f) * wscale[n] * xscale[0];
+    out_shift[n] = shift ? shift[n] : 0.0f;
+}
+
+// x = hi + lo with hi = bf16(x), lo = bf16(x - hi)
+__global__ void split_kernel(const float *__restrict__ in, long long n, bf16 *__restrict__ hi, bf16 *__restrict__ lo) {
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const float v = in[i];
+        const bf16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+__global__ void pack_split_kernel(const float *__restrict__ w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad,
+                                  bf16 *__restrict__ hi, bf16 *__restrict__ lo) {
+    const long long total = (long long) kn * Kpad;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x) {
+        const int co = (int) (i / Kpad), k = (int) (i % Kpad);
+        const int tap = k / Cp, ci = k % Cp;
+        float v = 0.0f;
+        if (tap < kh * kw && ci < C) v = wref(w, nchw, C, kh, kw, kn, ci, tap / kw, tap % kw, co);
+        const bf16 h = __float2bfloat16_rn(v);
+        hi[i] = h;
+        lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
 int grid_for(long long n) {
     long long g = (n + 255) / 256;
     return (int) (g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
@@ -153,5 +242,40 @@ cudaError_t prep_fold(int kn, const float *bias, const float *mean, const float 
 cudaError_t prep_to_bf16_nhwc(const float *in, int nchw, int B, int C, int H, int W, int Cp, void *out,
                               cudaStream_t st) {
     to_bf16_nhwc_kernel<<<grid_for((long long) B * H * W * Cp), 256, 0, st>>>(in, nchw, B, C, H, W, Cp, (bf16 *) out);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_fp8_quantize(long long n, int in_bf16, const void *in, void *out, float *scale, unsigned *amax_tmp,
+                              cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(amax_tmp, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    amax_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp);
+    quant_e4m3_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp, (uint8_t *) out, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_pack_fp8(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *out,
+                          float *wscale, cudaStream_t st) {
+    wscale_kernel<<<(kn + 127) / 128, 128, 0, st>>>(w, nchw, C * kh * kw, kn, wscale);
+    pack_fp8_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, wscale,
+                                                                    (uint8_t *) out);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_fp8_scales(int kn, const float *scale, const float *shift, const float *wscale, const float *xscale,
+                            float *out_scale, float *out_shift, cudaStream_t st) {
+    fp8_scales_kernel<<<(kn + 127) / 128, 128, 0, st>>>(kn, scale, shift, wscale, xscale, out_scale, out_shift);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_split(long long n, const float *in, void *hi, void *lo, cudaStream_t st) {
+    split_kernel<<<grid_for(n), 256, 0, st>>>(in, n, (bf16 *) hi, (bf16 *) lo);
+    return cudaGetLastError();
+}
+
+cudaError_t prep_pack_split(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *hi,
+                            void *lo, cudaStream_t st) {
+    pack_split_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, (bf16 *) hi,
+                                                                      (bf16 *) lo);
     return cudaGetLastError();
 }

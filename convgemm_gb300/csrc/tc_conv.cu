@@ -36,18 +36,31 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
+// Operand forms of the kernel.
+constexpr int MODE_BF16 = 0;  // BF16 x BF16, kind::f16
+constexpr int MODE_FP8 = 1;   // E4M3 x E4M3, kind::f8f6f4 (64-byte K rows, 64-byte swizzle)
+constexpr int MODE_X3 = 2;    // 3xBF16: hi*hi + hi*lo + lo*hi into one accumulator, FP32 output
+
 // KB 64-deep K blocks per pipeline stage: one full barrier and one MMA commit
 // cover KB blocks (a barrier round trip costs ~400 cycles, a 128 x 64 x 64 block
-// of MMAs ~150).
-template <int BN, int STAGES, int KB = 1>
+// of BF16 MMAs ~150).
+template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16>
 struct TcCfg {
-    static constexpr int BM = 128, BK = 64;
-    static constexpr uint32_t A_BLOCK = BM * BK * 2;   // one 64-deep block of A (128 rows x 128 B)
-    static constexpr uint32_t B_BLOCK = BN * BK * 2;
+    static constexpr int BM = 128, BK = 64;            // K elements per block
+    static constexpr int ROWB = MODE == MODE_FP8 ? 64 : 128;  // bytes of one K row of a block
+    static constexpr int NOPS = MODE == MODE_X3 ? 2 : 1;      // hi / lo copies of each operand
+    static constexpr uint32_t A_TILE = BM * ROWB;
+    static constexpr uint32_t B_TILE = BN * ROWB;
+    static constexpr uint32_t A_BLOCK = NOPS * A_TILE;
+    static constexpr uint32_t B_BLOCK = NOPS * B_TILE;
     static constexpr uint32_t A_BYTES = KB * A_BLOCK;
     static constexpr uint32_t B_BYTES = KB * B_BLOCK;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-    static constexpr uint32_t EPI_BYTES = BM * 64 * 2;  // one 128 x 64 BF16 output chunk
+    static constexpr uint32_t SBO = 8 * ROWB;                  // 8-row swizzle atom
+    static constexpr uint32_t LAYOUT = ROWB == 128 ? 2 : 4;    // SWIZZLE_128B / SWIZZLE_64B
+    static constexpr bool OUTF32 = MODE == MODE_X3;
+    static constexpr int CW = OUTF32 ? 32 : 64;                // output columns per 128-byte staging row
+    static constexpr uint32_t EPI_BYTES = BM * 128;            // one 128-row output chunk
     // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
     // MMA run ahead of the arrivals (LAG = STAGES - 1 would lock the two in step)
     static constexpr int LAG = STAGES / 2;
@@ -60,6 +73,12 @@ struct TcCfg {
     static_assert(SMEM <= 232448, "shared memory above the 227 KB per-block limit");
     static constexpr int THREADS = 288;
 };
+
+__device__ __forceinline__ uint64_t op_desc(uint32_t saddr, uint32_t sbo, uint32_t layout) {
+    uint64_t d = tc::sw128_desc(saddr, 16, sbo);
+    d &= ~((uint64_t) 7 << 61);
+    return d | ((uint64_t) layout << 61);
+}
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
@@ -104,12 +123,12 @@ __device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntile
     return tl;
 }
 
-template <int BN, int STAGES, int KB, bool IM2C>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE>
 __global__ void __launch_bounds__(288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
-    using C = TcCfg<BN, STAGES, KB>;
-    static_assert(IM2C || KB == 1, "the cp.async gather fills one K block per stage");
+    using C = TcCfg<BN, STAGES, KB, MODE>;
+    static_assert(IM2C || (KB == 1 && MODE == MODE_BF16), "the cp.async gather fills one BF16 K block per stage");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *epi_smem = base + STAGES * C::STAGE_BYTES;
@@ -141,7 +160,11 @@ __global__ void __launch_bounds__(288, 1)
         tc::prefetch_tmap(&wmap);
         if (p.epi_tma) tc::prefetch_tmap(&omap);
         if (IM2C)
-            for (int c = 0; c < p.ncls; c++) tc::prefetch_tmap(&amaps.a[c]);
+            for (int c = 0; c < p.ncls; c++) {
+                tc::prefetch_tmap(&amaps.a[c]);
+                if (MODE == MODE_X3) tc::prefetch_tmap(&amaps.alo[c]);
+            }
+        if (MODE == MODE_X3) tc::prefetch_tmap(&amaps.wlo);
     }
     for (int i = threadIdx.x; i < p.ncls * TC_MAXTAPS; i += blockDim.x) {
         const int c = i / TC_MAXTAPS, t = i % TC_MAXTAPS;
@@ -196,9 +219,15 @@ __global__ void __launch_bounds__(288, 1)
                         const int32_t to = taps[tap];
                         const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
                         const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
-                        tc::tma_load_im2col_4d(sa + kb * C::A_BLOCK, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
-                        tc::tma_load_2d(sa + C::A_BYTES + kb * C::B_BLOCK, &wmap, kbeg + (kt + kb) * C::BK, tl.n0,
-                                        &full[s]);
+                        const uint32_t ab = sa + kb * C::A_BLOCK, bb = sa + C::A_BYTES + kb * C::B_BLOCK;
+                        const int kcol = kbeg + (kt + kb) * C::BK;
+                        tc::tma_load_im2col_4d(ab, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
+                        tc::tma_load_2d(bb, &wmap, kcol, tl.n0, &full[s]);
+                        if (MODE == MODE_X3) {
+                            tc::tma_load_im2col_4d(ab + C::A_TILE, &amaps.alo[tl.cls], ci0, w0, h0, (int) b, offx, offy,
+                                                   &full[s]);
+                            tc::tma_load_2d(bb + C::B_TILE, &amaps.wlo, kcol, tl.n0, &full[s]);
+                        }
                         ci0 += 64;
                         if (ci0 == p.Cin) {
                             ci0 = 0;
@@ -303,42 +332,51 @@ __global__ void __launch_bounds__(288, 1)
             if (!ok) break;
             tc::tc_fence_after();
             const int m = tl.m0 + row;
-            bf16 *orow = nullptr;
+            uint8_t *orow = nullptr;   // this row of the output (BF16, or FP32 for MODE_X3)
             if (!p.epi_tma && m < M) {
                 uint32_t q, jw, j, b;
                 cl.dwg.divmod(m, q, jw);
                 cl.dhg.divmod(q, b, j);
                 const int oy = cl.oy0 + cl.osy * (int) j, ox = cl.ox0 + cl.osx * (int) jw;
-                orow = p.out + (((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout;
+                orow = (uint8_t *) p.out + ((((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout) * (C::OUTF32 ? 4 : 2);
             }
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 64) {
+            for (int c0 = 0; c0 < BN; c0 += C::CW) {
                 uint32_t v0[32], v1[32];
                 const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) (buf * BN + c0);
                 tc::tmem_ld_32x32b_x32(ta, v0);
-                tc::tmem_ld_32x32b_x32(ta + 32, v1);
+                if (C::CW == 64) tc::tmem_ld_32x32b_x32(ta + 32, v1);
                 tc::tmem_ld_wait();
-                if (c0 + 64 >= BN) {
+                if (c0 + C::CW >= BN) {
                     // the whole accumulator is in registers: hand the TMEM buffer back to the MMA warp
                     tc::tc_fence_before();
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
                 const int nb = tl.n0 + c0;
-                uint32_t pk[32];
+                uint32_t pk[32];   // one 128-byte output row chunk
+                if (C::OUTF32) {
 #pragma unroll
-                for (int jj = 0; jj < 32; jj++) {
-                    float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
-                    float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
-                    a = fmaf(a, scp[c0 + 2 * jj], shp[c0 + 2 * jj]);
-                    b = fmaf(b, scp[c0 + 2 * jj + 1], shp[c0 + 2 * jj + 1]);
-                    if (p.relu) {
-                        a = fmaxf(a, 0.0f);
-                        b = fmaxf(b, 0.0f);
+                    for (int jj = 0; jj < 32; jj++) {
+                        float a = fmaf(__uint_as_float(v0[jj]), scp[c0 + jj], shp[c0 + jj]);
+                        if (p.relu) a = fmaxf(a, 0.0f);
+                        pk[jj] = __float_as_uint(a);
                     }
-                    pk[jj] = pack_bf16x2(a, b);
+                } else {
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj++) {
+                        float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
+                        float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
+                        a = fmaf(a, scp[c0 + 2 * jj], shp[c0 + 2 * jj]);
+                        b = fmaf(b, scp[c0 + 2 * jj + 1], shp[c0 + 2 * jj + 1]);
+                        if (p.relu) {
+                            a = fmaxf(a, 0.0f);
+                            b = fmaxf(b, 0.0f);
+                        }
+                        pk[jj] = pack_bf16x2(a, b);
+                    }
                 }
                 if (p.epi_tma) {
-                    // 128 x 64 chunk through shared memory, stored by TMA (out-of-range rows/columns clipped)
+                    // 128-row chunk through shared memory, stored by TMA (out-of-range rows/columns clipped)
                     if (et == 0) {
                         if (C::EPI_BUFS == 2) bulk_wait_read<1>();
                         else bulk_wait_read<0>();
@@ -358,16 +396,22 @@ __global__ void __launch_bounds__(288, 1)
                     }
                     if (C::EPI_BUFS == 2) ebuf ^= 1;
                 } else if (orow && nb < p.Cout) {
-                    if (nb + 64 <= p.Cout) {
-                        uint4 *dst = reinterpret_cast<uint4 *>(orow + nb);
+                    if (nb + C::CW <= p.Cout) {
+                        uint4 *dst = reinterpret_cast<uint4 *>(orow + (size_t) nb * (C::OUTF32 ? 4 : 2));
 #pragma unroll
                         for (int q = 0; q < 8; q++) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+                    } else if (C::OUTF32) {
+                        float *o = reinterpret_cast<float *>(orow);
+#pragma unroll
+                        for (int jj = 0; jj < 32; jj++)
+                            if (nb + jj < p.Cout) o[nb + jj] = __uint_as_float(pk[jj]);
                     } else {
+                        bf16 *o = reinterpret_cast<bf16 *>(orow);
 #pragma unroll
                         for (int jj = 0; jj < 32; jj++) {
                             __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162 *>(&pk[jj]);
-                            if (nb + 2 * jj < p.Cout) orow[nb + 2 * jj] = h.x;
-                            if (nb + 2 * jj + 1 < p.Cout) orow[nb + 2 * jj + 1] = h.y;
+                            if (nb + 2 * jj < p.Cout) o[nb + 2 * jj] = h.x;
+                            if (nb + 2 * jj + 1 < p.Cout) o[nb + 2 * jj + 1] = h.y;
                         }
                     }
                 }
@@ -377,7 +421,7 @@ __global__ void __launch_bounds__(288, 1)
     } else {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
+            constexpr uint32_t idesc = MODE == MODE_FP8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, BN, 0, 0);
             uint32_t it = 0, lt = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
                 const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
@@ -401,11 +445,24 @@ __global__ void __launch_bounds__(288, 1)
                     const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
                     const uint32_t b0 = a0 + C::A_BYTES;
                     for (int kb = 0; kb < nkb; kb++) {
+                        const uint32_t ab = a0 + kb * C::A_BLOCK, bb = b0 + kb * C::B_BLOCK;
+                        // each MMA consumes 32 bytes of every K row: 16 BF16 or 32 E4M3 elements
 #pragma unroll
-                        for (int k = 0; k < C::BK / 16; k++) {
-                            const uint64_t ad = tc::sw128_desc(a0 + kb * C::A_BLOCK + k * 32, 16, 1024);
-                            const uint64_t bd = tc::sw128_desc(b0 + kb * C::B_BLOCK + k * 32, 16, 1024);
-                            tc::mma_f16(dt, ad, bd, idesc, (kt | kb | k) != 0);
+                        for (int k = 0; k < C::ROWB / 32; k++) {
+                            const uint32_t acc = (kt | kb | k) != 0;
+                            const uint64_t ad = op_desc(ab + k * 32, C::SBO, C::LAYOUT);
+                            const uint64_t bd = op_desc(bb + k * 32, C::SBO, C::LAYOUT);
+                            if (MODE == MODE_FP8) {
+                                tc::mma_f8(dt, ad, bd, idesc, acc);
+                            } else {
+                                tc::mma_f16(dt, ad, bd, idesc, acc);
+                                if (MODE == MODE_X3) {
+                                    const uint64_t adl = op_desc(ab + C::A_TILE + k * 32, C::SBO, C::LAYOUT);
+                                    const uint64_t bdl = op_desc(bb + C::B_TILE + k * 32, C::SBO, C::LAYOUT);
+                                    tc::mma_f16(dt, ad, bdl, idesc, 1);   // hi * lo
+                                    tc::mma_f16(dt, adl, bd, idesc, 1);   // lo * hi
+                                }
+                            }
                         }
                     }
                     tc::mma_commit(&empty[s]);
@@ -422,11 +479,11 @@ __global__ void __launch_bounds__(288, 1)
     if (warp == 8) tc::tmem_dealloc(tmem, 2 * BN);
 }
 
-template <int BN, int STAGES, int KB, bool IM2C>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE>
 cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
                       int grid, cudaStream_t st) {
-    using C = TcCfg<BN, STAGES, KB>;
-    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C>;
+    using C = TcCfg<BN, STAGES, KB, MODE>;
+    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -439,23 +496,40 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUte
 
 }  // namespace
 
-// Stage shapes (all ~192 KB of ring): im2col path BN=64: 4 stages of 2 K blocks;
-// BN=128: 3 stages of 2 blocks; BN=256: 3 stages of 1 block with two output staging
-// buffers (its tiles are often single-block 1x1 layers bound by the output stores).
+// Stage shapes (~192 KB of ring each).  BF16 im2col: BN=64 4 stages of 2 K blocks,
+// BN=128 3 x 2, BN=256 3 x 1 with two output staging buffers (its tiles are often
+// single-block 1x1 layers bound by the output stores).  FP8 blocks are half the bytes,
+// 3xBF16 blocks twice.
 cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
                            const TcMaps &amaps, int grid, cudaStream_t st) {
+    if (p.mode == MODE_FP8) {
+        switch (p.bn) {
+            case 64: return launch_bn<64, 4, 4, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 3, 4, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 2, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (p.mode == MODE_X3) {
+        switch (p.bn) {
+            case 64: return launch_bn<64, 4, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 3, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 2, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
     if (p.im2col) {
         switch (p.bn) {
-            case 64: return launch_bn<64, 4, 2, true>(p, wmap, omap, amaps, grid, st);
-            case 128: return launch_bn<128, 3, 2, true>(p, wmap, omap, amaps, grid, st);
-            case 256: return launch_bn<256, 3, 1, true>(p, wmap, omap, amaps, grid, st);
+            case 64: return launch_bn<64, 4, 2, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 3, 2, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 1, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);
             default: return cudaErrorInvalidValue;
         }
     }
     switch (p.bn) {
-        case 64: return launch_bn<64, 8, 1, false>(p, wmap, omap, amaps, grid, st);
-        case 128: return launch_bn<128, 6, 1, false>(p, wmap, omap, amaps, grid, st);
-        case 256: return launch_bn<256, 4, 1, false>(p, wmap, omap, amaps, grid, st);
+        case 64: return launch_bn<64, 8, 1, false, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+        case 128: return launch_bn<128, 6, 1, false, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+        case 256: return launch_bn<256, 4, 1, false, MODE_BF16>(p, wmap, omap, amaps, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -43,6 +43,7 @@ struct TcConvParams {
     int epi_tma;               // output pixels are the GEMM rows in order: stage in SMEM, TMA store
     int im2col;                // A loaded by im2col-mode TMA (Cin % 64 == 0), else gathered by cp.async
     int cpb;                   // 64-channel chunks per tap (Cin / 64) on the im2col path
+    int mode;                  // 0 BF16, 1 FP8-E4M3, 2 3xBF16 (FP32 output)
     int ncls;
     TcClass cls[TC_MAXCLS];
 };
@@ -50,7 +51,9 @@ struct TcConvParams {
 constexpr int TC_MAXIM2COL = 4;  // classes that can use im2col-mode TMA in one launch
 
 struct TcMaps {
-    CUtensorMap a[TC_MAXIM2COL];  // im2col maps of the gathered tensor, one per class
+    CUtensorMap a[TC_MAXIM2COL];    // im2col maps of the gathered tensor, one per class
+    CUtensorMap alo[TC_MAXIM2COL];  // 3xBF16: maps of the low parts
+    CUtensorMap wlo;                // 3xBF16: packed low parts of the weights
 };
 
 // wmap: packed weights [Cout][K] (box 64 x bn); omap: output [pixels][Cout] (box 64 x 128), used when epi_tma.

@@ -58,18 +58,22 @@ EncodeIm2colFn encode_im2col_fn() {
 // im2col-mode map of a BF16 NHWC tensor [B][H][W][C]: `pixels` pixels x 64 channels per load,
 // bounding box [lo, dim-1+up] per spatial dimension, traversal strides (sh, sw), 128-byte swizzle.
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
-                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels) {
+                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes) {
     EncodeIm2colFn fn = encode_im2col_fn();
     if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col is unavailable");
-    if (((uintptr_t) ptr & 15) || (C * 2) % 16)
+    if (((uintptr_t) ptr & 15) || (C * elem_bytes) % 16)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "im2col operand not 16-byte aligned");
+    const cuuint64_t eb = (cuuint64_t) elem_bytes;
     cuuint64_t dims[4] = {(cuuint64_t) C, (cuuint64_t) W, (cuuint64_t) H, (cuuint64_t) B};
-    cuuint64_t strides[3] = {(cuuint64_t) C * 2, (cuuint64_t) W * C * 2, (cuuint64_t) H * W * C * 2};
+    cuuint64_t strides[3] = {(cuuint64_t) C * eb, (cuuint64_t) W * C * eb, (cuuint64_t) H * W * C * eb};
     int lower[2] = {lo_w, lo_h};
     int upper[2] = {up_w, up_h};
     cuuint32_t estr[4] = {1, (cuuint32_t) sw, (cuuint32_t) sh, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, lower, upper, 64,
-                    (cuuint32_t) pixels, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    // 64 channels per pixel: 128 B rows (BF16, 128-byte swizzle) or 64 B rows (E4M3, 64-byte swizzle)
+    CUresult r = fn(map, elem_bytes == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                    const_cast<void *>(ptr), dims, strides, lower, upper, 64, (cuuint32_t) pixels, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    elem_bytes == 1 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col failed (%d)", (int) r);
     return CONVGEMM_SUCCESS;
@@ -104,6 +108,11 @@ bool tc_plan_im2col(TcPlan &pl) {
 // 2-D row-major [rows][cols] tensor, box {64 (cols), box_rows}, 128-byte swizzle.
 convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
                                  long long rows, long long cols, int box_cols, int box_rows) {
+    return tc_make_map_2d_sw(map, dt, elem_bytes, ptr, rows, cols, box_cols, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
+convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
+                                    long long rows, long long cols, int box_cols, int box_rows, CUtensorMapSwizzle sw) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     if (((uintptr_t) ptr & 15) || ((cols * elem_bytes) & 15))
@@ -112,8 +121,8 @@ convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int e
     cuuint64_t strides[1] = {(cuuint64_t) cols * elem_bytes};
     cuuint32_t box[2] = {(cuuint32_t) box_cols, (cuuint32_t) box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = fn(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int) r);
     return CONVGEMM_SUCCESS;
 }
@@ -266,23 +275,30 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 }
 
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
-                         const float *scale, const float *shift, int relu, cudaStream_t st) {
+                         const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
+                         const void *in_lo, const void *w_lo) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
     TcConvParams p;
     memset(&p, 0, sizeof(p));
+    p.mode = mode;
     p.bn = tc_pick_bn(pl, sms);
+    const int eb = mode == 1 ? 1 : 2;   // operand element bytes
     CUtensorMap wmap, omap;
-    if (convgemm_status_t e =
-            tc_make_map_2d(&wmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wpacked, pl.Cout, pl.Ktot, 64, p.bn))
+    if (convgemm_status_t e = tc_make_map_2d_sw(&wmap, eb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                                                eb, wpacked, pl.Cout, pl.Ktot, 64, p.bn,
+                                                eb == 1 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B))
         return e;
     const TcClass &c0 = pl.cls[0];
     p.epi_tma = pl.ncls == 1 && c0.osy == 1 && c0.osx == 1 && c0.oy0 == 0 && c0.ox0 == 0 && c0.Hg == pl.Hout &&
                 c0.Wg == pl.Wout && (pl.Cout % 8) == 0 && ((uintptr_t) out & 15) == 0;
     memset(&omap, 0, sizeof(omap));
     if (p.epi_tma) {
-        if (convgemm_status_t e = tc_make_map_2d(&omap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, out,
-                                                 (long long) s.b * pl.Hout * pl.Wout, pl.Cout, 64, 128))
+        // 128-byte rows of output: 64 BF16 or 32 FP32 (3xBF16) channels
+        const bool f32 = mode == 2;
+        if (convgemm_status_t e = tc_make_map_2d(&omap, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                                                 f32 ? 4 : 2, out, (long long) s.b * pl.Hout * pl.Wout, pl.Cout,
+                                                 f32 ? 32 : 64, 128))
             return e;
     }
     p.in = (const __nv_bfloat16 *) in;
@@ -306,6 +322,9 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     TcMaps amaps;
     memset(&amaps, 0, sizeof(amaps));
     p.im2col = tc_plan_im2col(pi);
+    if (mode != 0 && !p.im2col)
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED,
+                            "FP8 / 3xBF16 forms need channels a multiple of 64 (im2col-mode TMA)");
     if (p.im2col) {
         p.cpb = pl.Cin / 64;
         for (int c = 0; c < pi.ncls; c++) {
@@ -313,9 +332,17 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
             const int up_y = cl.lo_y + (cl.Hg - 1) * cl.isy - (pl.Hin - 1);
             const int up_x = cl.lo_x + (cl.Wg - 1) * cl.isx - (pl.Win - 1);
             if (convgemm_status_t e = tc_make_im2col_map(&amaps.a[c], in, s.b, pl.Hin, pl.Win, pl.Cin, cl.lo_y,
-                                                         cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128))
+                                                         cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, eb))
                 return e;
+            if (mode == 2)
+                if (convgemm_status_t e = tc_make_im2col_map(&amaps.alo[c], in_lo, s.b, pl.Hin, pl.Win, pl.Cin,
+                                                             cl.lo_y, cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, 2))
+                    return e;
         }
+        if (mode == 2)
+            if (convgemm_status_t e =
+                    tc_make_map_2d(&amaps.wlo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, w_lo, pl.Cout, pl.Ktot, 64, p.bn))
+                return e;
     }
     int t0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
@@ -537,7 +564,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
                    up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
         if (p.im2col)
             if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
-                                                         s.vstride, s.hstride, 64))
+                                                         s.vstride, s.hstride, 64, 2))
                 return e;
     }
     cudaStream_t st = (cudaStream_t) stream;

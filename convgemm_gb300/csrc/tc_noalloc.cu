@@ -147,7 +147,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
                    up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
         if (p.im2col)
             if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
-                                                         s.vstride, s.hstride, 64))
+                                                         s.vstride, s.hstride, 64, 2))
                 return e;
     }
     cudaStream_t st = (cudaStream_t) stream;

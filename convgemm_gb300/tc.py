@@ -52,3 +52,44 @@ def wgrad_bf16(layout, shape: Shape, dy, x, dw, workspace, stream=None):
     nbytes = workspace.numel() * workspace.element_size()
     _raise_if(lib().convgemm_wgrad_bf16(layout, ctypes.byref(shape), ptr(dy), ptr(x), ptr(dw), ptr(workspace),
                                         nbytes, _stream(stream)))
+
+
+# ------------------------------------------------------------- FP8-E4M3 form
+def fp8_quantize(x, out, scale2, stream=None):
+    """Per-tensor E4M3 quantisation; scale2 is a 2-float device tensor (scale, scratch)."""
+    in_bf16 = 1 if str(x.dtype) == "torch.bfloat16" else 0
+    _raise_if(lib().convgemm_fp8_quantize(x.numel(), in_bf16, ptr(x), ptr(out), ptr(scale2), _stream(stream)))
+
+
+def fp8_weights_size(shape: Shape) -> int:
+    return lib().convgemm_fp8_weights_size(ctypes.byref(shape))
+
+
+def fp8_pack_weights(layout, shape: Shape, weights, packed, wscale, stream=None):
+    _raise_if(lib().convgemm_fp8_pack_weights(layout, ctypes.byref(shape), ptr(weights), ptr(packed), ptr(wscale),
+                                              _stream(stream)))
+
+
+def fp8_epilogue_scales(kn, scale, shift, wscale, xscale, out_scale, out_shift, stream=None):
+    _raise_if(lib().convgemm_fp8_epilogue_scales(kn, ptr(scale), ptr(shift), ptr(wscale), ptr(xscale),
+                                                 ptr(out_scale), ptr(out_shift), _stream(stream)))
+
+
+def fwd_fp8(shape: Shape, x, wpacked, y, scale, shift=None, relu=False, stream=None):
+    _raise_if(lib().convgemm_fwd_fp8(ctypes.byref(shape), ptr(x), ptr(wpacked), ptr(y), ptr(scale), ptr(shift),
+                                     int(bool(relu)), _stream(stream)))
+
+
+# ------------------------------------------------------------- 3xBF16 form
+def split_bf16x2(x, hi, lo, stream=None):
+    _raise_if(lib().convgemm_split_bf16x2(x.numel(), ptr(x), ptr(hi), ptr(lo), _stream(stream)))
+
+
+def bf16x3_pack_weights(layout, shape: Shape, weights, hi, lo, stream=None):
+    _raise_if(lib().convgemm_bf16x3_pack_weights(layout, ctypes.byref(shape), ptr(weights), ptr(hi), ptr(lo),
+                                                 _stream(stream)))
+
+
+def fwd_bf16x3(shape: Shape, x_hi, x_lo, w_hi, w_lo, y, scale=None, shift=None, relu=False, stream=None):
+    _raise_if(lib().convgemm_fwd_bf16x3(ctypes.byref(shape), ptr(x_hi), ptr(x_lo), ptr(w_hi), ptr(w_lo), ptr(y),
+                                        ptr(scale), ptr(shift), int(bool(relu)), _stream(stream)))

@@ -125,6 +125,43 @@ convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, const void *x
 convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
                                       void *stream);
 
+/* ------------------------------------------- FP8-E4M3 and 3xBF16 forward forms */
+
+/* Per-tensor E4M3 quantisation of n contiguous values (BF16 if in_is_bf16, else FP32):
+ * scale[0] = amax/448, out = e4m3(in/scale[0]); scale must hold 2 floats (scale[1] is scratch). */
+convgemm_status_t convgemm_fp8_quantize(size_t n, int in_is_bf16, const void *in, void *out, float *scale,
+                                        void *stream);
+
+/* Bytes of the packed E4M3 weight operand ([kn][taps*c], K padded to 64). */
+size_t convgemm_fp8_weights_size(const convgemm_shape_t *shape);
+
+/* Per-output-channel E4M3 weights: wscale[n] = amax_n/448, packed = e4m3(w/wscale[n]). */
+convgemm_status_t convgemm_fp8_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                            const float *weights, void *packed, float *wscale, void *stream);
+
+/* Folds the quantisation scales into the epilogue: out_scale[n] = scale[n]*wscale[n]*xscale[0],
+ * out_shift[n] = shift[n] (scale/shift from convgemm_fold_epilogue, or NULL for 1/0). */
+convgemm_status_t convgemm_fp8_epilogue_scales(int kn, const float *scale, const float *shift, const float *wscale,
+                                               const float *xscale, float *out_scale, float *out_shift, void *stream);
+
+/* Forward, E4M3 x E4M3 tensor cores (tcgen05 kind::f8f6f4), FP32 accumulation:
+ * x E4M3 NHWC [b][h][w][c], y BF16 NHWC = relu?(acc*scale + shift).  Needs c % 64 == 0. */
+convgemm_status_t convgemm_fwd_fp8(const convgemm_shape_t *shape, const void *x, const void *wpacked, void *y,
+                                   const float *scale, const float *shift, int relu, void *stream);
+
+/* x = hi + lo, both BF16 (hi = bf16(x), lo = bf16(x - hi)), n contiguous FP32 values. */
+convgemm_status_t convgemm_split_bf16x2(size_t n, const float *in, void *hi, void *lo, void *stream);
+
+/* Packed hi/lo BF16 weight operands (each convgemm_bf16_weights_size(shape, CONVGEMM_OPERAND_FWD) bytes). */
+convgemm_status_t convgemm_bf16x3_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                               const float *weights, void *hi, void *lo, void *stream);
+
+/* Forward with 3xBF16 split products (hi*hi + hi*lo + lo*hi accumulated in FP32):
+ * x_hi/x_lo BF16 NHWC [b][h][w][c]; y FP32 NHWC.  Needs c % 64 == 0. */
+convgemm_status_t convgemm_fwd_bf16x3(const convgemm_shape_t *shape, const void *x_hi, const void *x_lo,
+                                      const void *w_hi, const void *w_lo, float *y, const float *scale,
+                                      const float *shift, int relu, void *stream);
+
 /* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
 size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);
 
