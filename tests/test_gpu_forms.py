@@ -22,7 +22,7 @@ SHAPES = [
     (2, 8, 8, 256, 512, 1, 0, 1, 1),
     (1, 13, 11, 64, 72, 3, 2, 1, 2),
 ]
-FP8_TOL_MAX, FP8_TOL_RMS = 8e-2, 3e-2   # E4M3 carries 3 mantissa bits
+FP8_TOL_MAX, FP8_TOL_RMS = 8e-2, 5e-2   # E4M3 carries 3 mantissa bits
 FP8_SELF_TOL = 6e-3                      # vs FP64 of the dequantised operands
 X3_TOL = 1e-4                            # 3xBF16 vs FP64 of the FP32 inputs
 
