@@ -348,6 +348,159 @@ def timed(torch, fn, steps, warmup, stream):
     return start.elapsed_time(end) / steps
 
 
+def grouped_cpu_baseline(specs, every=8, threads=None):
+    """The oracle port (FP32 sconvGemmNHWC in the reference's order) on every `every`-th
+    convolution of the grouped workload.  Returns (seconds, flops)."""
+    import numpy as np
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    rng = np.random.default_rng(1)
+    t_total, fl = 0.0, 0
+    for d in specs[::every]:
+        g = dict(b=d["b"], h=d["h"], w=d["w"], c=d["c"], kn=d["kn"], kh=d["k"], kw=d["k"], vpad=d["pad"],
+                 hpad=d["pad"], vstr=d["stride"], hstr=d["stride"], vdil=1, hdil=1)
+        ho = (d["h"] + 2 * d["pad"] - d["k"]) // d["stride"] + 1
+        K = d["c"] * d["k"] * d["k"]
+        x = rng.uniform(-1, 1, d["b"] * d["h"] * d["w"] * d["c"]).astype(np.float32)
+        w = (rng.standard_normal(K * d["kn"]) * np.sqrt(2.0 / K)).astype(np.float32)
+        epi = {"bias": rng.uniform(-.1, .1, d["kn"]).astype(np.float32), "relu": True}
+        y = np.empty(d["b"] * ho * ho * d["kn"], np.float32)
+        t0 = time.perf_counter()
+        O.call_fwd("port", O.NHWC, g, w, x, y, epi)
+        t_total += time.perf_counter() - t0
+        fl += 2 * d["b"] * ho * ho * d["kn"] * K
+    return t_total, fl
+
+
+def run_grouped(args):
+    """256 independent uneven BF16 convolutions (bias + ReLU): one persistent grouped launch
+    in a CUDA graph, against one launch per convolution (also in a CUDA graph)."""
+    import torch
+    import convgemm_gb300 as cg
+    from convgemm_gb300 import autotune, tc
+    from convgemm_gb300.workloads import uneven_convs
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cg.lib()
+    specs = uneven_convs(args.group_n, 2024)
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    convs, singles, flops = [], [], 0
+    in_bytes = out_bytes = 0
+    for d in specs:
+        s = cg.Shape.of(d["b"], d["h"], d["w"], d["c"], d["kn"], d["k"], d["k"], d["pad"], d["pad"],
+                        d["stride"], d["stride"], 1, 1)
+        K = d["c"] * d["k"] * d["k"]
+        x = (torch.rand(d["b"], d["h"], d["w"], d["c"], device="cuda", generator=gen) * 2 - 1).to(torch.bfloat16)
+        w32 = torch.randn(K * d["kn"], device="cuda", generator=gen) * (2.0 / K) ** 0.5
+        bias = torch.rand(d["kn"], device="cuda", generator=gen) * 0.2 - 0.1
+        wp = torch.empty(tc.group_weights_size(s) // 2, dtype=torch.bfloat16, device="cuda")
+        tc.group_pack_weights(cg.NHWC, s, w32, wp)
+        ws = torch.empty(tc.weights_size(s, tc.OPERAND_FWD) // 2, dtype=torch.bfloat16, device="cuda")
+        tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, w32, ws)
+        y = torch.empty(d["b"], s.ho, s.wo, d["kn"], dtype=torch.bfloat16, device="cuda")
+        y1 = torch.empty_like(y)
+        convs.append(dict(shape=s, x=x, w=wp, y=y, shift=bias, relu=True))
+        singles.append((s, x, ws, y1, bias))
+        flops += 2 * d["b"] * s.ho * s.wo * d["kn"] * K
+        in_bytes += x.numel() * 2
+        out_bytes += y.numel() * 2
+    torch.cuda.synchronize()
+
+    t0 = time.perf_counter()
+    widths = autotune.tune(convs)
+    tune_s = time.perf_counter() - t0
+    grp = tc.Group(convs)
+    default_grp = tc.Group([dict(c, bn=autotune.default_width(c["shape"].kn)) for c in convs])
+
+    def per_conv():
+        for (s, x, ws, y1, bias) in singles:
+            tc.fwd_bf16(s, x, ws, y1, None, bias, relu=True)
+
+    stream = torch.cuda.Stream()
+    graphs = {}
+    for name, fn in (("grouped", grp.launch), ("grouped_default_widths", default_grp.launch),
+                     ("per_conv", per_conv)):
+        with torch.cuda.stream(stream):
+            fn()
+            stream.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                fn()
+        graphs[name] = g
+    torch.cuda.synchronize()
+    cg.check_device()
+    diff = max(((a["y"].float() - b[3].float()).abs().max() / b[3].float().abs().max().clamp_min(1e-30)).item()
+               for a, b in zip(convs, singles))
+
+    clocks = ClockSampler(local)
+    ms = timed(torch, graphs["grouped"].replay, args.steps, args.warmup, torch.cuda.current_stream())
+    clk = clocks.stop()
+    times = {"grouped": ms}
+    for name in ("grouped_default_widths", "per_conv"):
+        times[name] = timed(torch, graphs[name].replay, args.steps, args.warmup, torch.cuda.current_stream())
+    times["per_conv_eager"] = timed(torch, per_conv, max(3, args.steps // 2), 1, torch.cuda.current_stream())
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    cg.check_device()
+    value = world * flops / (ms / 1000) / 1e12
+
+    # e2e: inputs from pinned host memory, one grouped launch, outputs back to pinned host memory
+    xh = [torch.empty(c["x"].shape, dtype=torch.bfloat16).pin_memory() for c in convs]
+    yh = [torch.empty(c["y"].shape, dtype=torch.bfloat16).pin_memory() for c in convs]
+    for a, c in zip(xh, convs):
+        a.copy_(c["x"])
+
+    def e2e_step():
+        for a, c in zip(xh, convs):
+            c["x"].copy_(a, non_blocking=True)
+        grp.launch()
+        for a, c in zip(yh, convs):
+            a.copy_(c["y"], non_blocking=True)
+
+    e2e_ms = timed(torch, e2e_step, max(3, args.steps // 2), 1, torch.cuda.current_stream())
+    peaks, peak_kind = read_peaks()
+    roof = {"bound": "tensor", "kernel": "tc_group_kernel", "achieved": value / world, "peak": peaks["bf16_tflops"],
+            "unit": "TFLOP/s", "frac": value / world / peaks["bf16_tflops"], "traffic": None,
+            "peak_source": f"{peak_kind} bf16_tflops (burst: one launch timed alone)",
+            "how": "algorithmic FLOPs (2*b*ho*wo*kn*c*k*k summed over the convolutions) / CUDA-event time of one "
+                   "graph replay of the single grouped launch"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t, fl = grouped_cpu_baseline(specs, 8, os.cpu_count())
+        cpu = {"value": fl / t / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"every 8th convolution ({len(specs[::8])} of {len(specs)}) in FP32, "
+                         "sconvGemmNHWC of the oracle port"}
+    if rank == 0:
+        hist = {str(w): widths.count(w) for w in sorted(set(widths))}
+        line = {"metric": "grouped uneven convolutions: TFLOP/s of one persistent launch", "value": value,
+                "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16", "data": "synthetic",
+                "config": {"workload": f"{len(specs)} seeded uneven NHWC BF16 forward convs (batch 1-32, "
+                                       "H=W in 7..112, Ci/Co 16..512 step 16, k 1/3/5, stride 1/2, pad k/2), "
+                                       "bias + ReLU",
+                           "gflop_per_step": flops / 1e9, "input_gb": in_bytes / 1e9, "output_gb": out_bytes / 1e9,
+                           "l2": "inputs larger than L2", "parallelism": f"replicas{world}",
+                           "tile_widths": hist, "autotune_s": tune_s},
+                "times_ms": times, "speedup_vs_per_conv_graph": times["per_conv"] / ms,
+                "max_rel_diff_vs_per_conv": diff, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": {"value": world * flops / (e2e_ms / 1000) / 1e12, "unit": "TFLOP/s",
+                        "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms},
+                "clocks": clk, "gpu_launches": args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,10 +517,15 @@ def main():
     ap.add_argument("--only", default=None,
                     help="LAYER:OP (e.g. s3b2_conv2:fwd): run just that BF16 op, eagerly, warmup+steps times "
                          "(for profiler captures)")
+    ap.add_argument("--workload", default="resnet50", choices=["resnet50", "grouped"],
+                    help="resnet50: the headline fwd+bwd step; grouped: uneven convolutions in one launch")
+    ap.add_argument("--group-n", type=int, default=256)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "grouped":
+        return run_grouped(args)
 
     import torch
     import convgemm_gb300 as cg

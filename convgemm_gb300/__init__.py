@@ -115,6 +115,13 @@ def lib():
         L.convgemm_split_bf16x2.argtypes = [ctypes.c_size_t, _VP, _VP, _VP, _VP]
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
+        L.convgemm_group_weights_size.argtypes = [SP]
+        L.convgemm_group_weights_size.restype = ctypes.c_size_t
+        L.convgemm_group_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP]
+        L.convgemm_group_table_size.argtypes = [_I]
+        L.convgemm_group_table_size.restype = ctypes.c_size_t
+        L.convgemm_group_prepare.argtypes = [_I, _VP, _VP, ctypes.c_size_t, ctypes.POINTER(_I)]
+        L.convgemm_group_launch.argtypes = [_VP, _I, _I, _VP]
         _lib = L
     return _lib
 

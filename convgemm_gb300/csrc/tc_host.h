@@ -26,6 +26,7 @@ convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, in
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
 bool tc_plan_im2col(TcPlan &pl);
+int tc_num_sms();
 // mode: 0 BF16, 1 FP8-E4M3 (in/wpacked are E4M3), 2 3xBF16 (in_lo/w_lo low parts, FP32 output)
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,

@@ -93,3 +93,49 @@ def bf16x3_pack_weights(layout, shape: Shape, weights, hi, lo, stream=None):
 def fwd_bf16x3(shape: Shape, x_hi, x_lo, w_hi, w_lo, y, scale=None, shift=None, relu=False, stream=None):
     _raise_if(lib().convgemm_fwd_bf16x3(ctypes.byref(shape), ptr(x_hi), ptr(x_lo), ptr(w_hi), ptr(w_lo), ptr(y),
                                         ptr(scale), ptr(shift), int(bool(relu)), _stream(stream)))
+
+
+# ------------------------------------------------ grouped persistent forward launch
+class GroupConv(ctypes.Structure):
+    """convgemm_group_conv_t (include/convgemm_gpu.h)."""
+    _fields_ = [("shape", Shape), ("x", ctypes.c_void_p), ("w", ctypes.c_void_p), ("y", ctypes.c_void_p),
+                ("scale", ctypes.c_void_p), ("shift", ctypes.c_void_p), ("relu", ctypes.c_int), ("bn", ctypes.c_int)]
+
+
+def group_weights_size(shape: Shape) -> int:
+    return lib().convgemm_group_weights_size(ctypes.byref(shape))
+
+
+def group_pack_weights(layout, shape: Shape, weights, packed, stream=None):
+    _raise_if(lib().convgemm_group_pack_weights(layout, ctypes.byref(shape), ptr(weights), ptr(packed),
+                                                _stream(stream)))
+
+
+class Group:
+    """Many BF16 NHWC forward convolutions run by one persistent launch.
+
+    convs: sequence of dicts with keys shape, x, w (packed by group_pack_weights),
+    y, and optionally scale, shift, relu, bn (64/128/256 output channels per tile;
+    0 lets the library choose).  The tensor maps are encoded once here; launch()
+    may be captured in a CUDA graph.  The tensors must stay alive and in place.
+    """
+
+    def __init__(self, convs, device="cuda"):
+        import torch
+        n = len(convs)
+        arr = (GroupConv * n)()
+        for i, c in enumerate(convs):
+            arr[i] = GroupConv(c["shape"], ptr(c["x"]), ptr(c["w"]), ptr(c["y"]), ptr(c.get("scale")),
+                               ptr(c.get("shift")), int(bool(c.get("relu", False))), int(c.get("bn", 0)))
+        nbytes = lib().convgemm_group_table_size(n)
+        self.table = torch.empty(nbytes + 64, dtype=torch.uint8, device=device)
+        off = (-self.table.data_ptr()) % 64
+        self._tptr = self.table.data_ptr() + off
+        tiles = ctypes.c_int(0)
+        _raise_if(lib().convgemm_group_prepare(n, ctypes.cast(arr, ctypes.c_void_p), self._tptr, nbytes,
+                                               ctypes.byref(tiles)))
+        self.n, self.tiles = n, tiles.value
+        self._keep = convs
+
+    def launch(self, stream=None):
+        _raise_if(lib().convgemm_group_launch(self._tptr, self.n, self.tiles, _stream(stream)))

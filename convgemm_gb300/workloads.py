@@ -45,3 +45,19 @@ def conv_flops(layer, batch):
     """2*b*ho*wo*kn*c*k*k: the reference's 2*M*N*K (plots/convgemm.plt:56); the same for fwd, dgrad, wgrad."""
     ho, wo = out_hw(layer)
     return 2 * batch * ho * wo * layer["kn"] * layer["c"] * layer["k"] * layer["k"]
+
+
+def uneven_convs(n=256, seed=2024):
+    """Seeded independent convolutions of uneven shapes for the grouped launch:
+    batch 1-32, H = W in {7, 14, 28, 56, 112}, input/output channels in
+    {16, 32, ..., 512}, kernel 1/3/5, stride 1/2, pad = k // 2 (NHWC, BF16,
+    fused bias + ReLU).  Returns dicts with b, h, w, c, kn, k, stride, pad."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        k = int(rng.choice([1, 3, 5]))
+        h = int(rng.choice([7, 14, 28, 56, 112]))
+        out.append(dict(b=int(rng.integers(1, 33)), h=h, w=h, c=16 * int(rng.integers(1, 33)),
+                        kn=16 * int(rng.integers(1, 33)), k=k, stride=int(rng.choice([1, 2])), pad=k // 2))
+    return out

@@ -162,6 +162,39 @@ convgemm_status_t convgemm_fwd_bf16x3(const convgemm_shape_t *shape, const void 
                                       const void *w_hi, const void *w_lo, float *y, const float *scale,
                                       const float *shift, int relu, void *stream);
 
+/* ----------------------------------------- grouped persistent forward launch */
+
+/* One convolution of a grouped launch: BF16 NHWC x [b][h][w][c] (c % 8 == 0),
+ * weights packed by convgemm_group_pack_weights, BF16 NHWC y [b][ho][wo][kn] =
+ * relu?(acc*scale + shift) (scale/shift may be NULL); bn = output channels per
+ * tile (64, 128 or 256; 0 = chosen from kn), e.g. from the autotuner. */
+typedef struct {
+    convgemm_shape_t shape;
+    const void *x;
+    const void *w;
+    void *y;
+    const float *scale;
+    const float *shift;
+    int relu;
+    int bn;
+} convgemm_group_conv_t;
+
+/* Packed weights of a grouped-launch convolution: [kn][taps * c64], c64 = c rounded up to 64. */
+size_t convgemm_group_weights_size(const convgemm_shape_t *shape);
+convgemm_status_t convgemm_group_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape,
+                                              const float *weights, void *packed, void *stream);
+
+/* Bytes of the device problem table of n convolutions (64-byte aligned memory). */
+size_t convgemm_group_table_size(int n);
+
+/* Encodes the tensor maps of n convolutions into the device table (synchronous
+ * copy; do it once, outside any stream capture) and returns the tile count. */
+convgemm_status_t convgemm_group_prepare(int n, const convgemm_group_conv_t *convs, void *table, size_t table_bytes,
+                                         int *total_tiles);
+
+/* All n convolutions in one persistent launch (capturable in a CUDA graph). */
+convgemm_status_t convgemm_group_launch(const void *table, int n, int total_tiles, void *stream);
+
 /* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
 size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);
 

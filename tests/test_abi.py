@@ -80,3 +80,18 @@ def test_workspace_size_query(cglib):
     n = cglib.wgrad_f32_workspace_size(s)
     nblocks = -(-(2 * 10 * 10) // 384)
     assert n == 4 * nblocks * 36 * 8
+
+
+def test_group_prepare_rejects_bad_arguments_without_gpu(cglib):
+    from convgemm_gb300 import tc
+    L = cglib.lib()
+    tiles = ctypes.c_int(0)
+    assert L.convgemm_group_prepare(0, None, None, 0, ctypes.byref(tiles)) == 1
+    s = cglib.Shape.of(1, 8, 8, 12, 16, 3, 3, 1, 1)   # c % 8 != 0
+    assert L.convgemm_group_weights_size(ctypes.byref(s)) == 0
+    conv = tc.GroupConv(s, 16, 16, 16, None, None, 0, 0)
+    buf = ctypes.create_string_buffer(L.convgemm_group_table_size(1) + 64)
+    addr = (ctypes.addressof(buf) + 63) // 64 * 64
+    st = L.convgemm_group_prepare(1, ctypes.addressof(conv), addr, L.convgemm_group_table_size(1), ctypes.byref(tiles))
+    assert st != 0 and "c % 8" in cglib.last_error()[1]
+    assert L.convgemm_group_table_size(4) == 4 * L.convgemm_group_table_size(1) > 0
