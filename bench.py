@@ -48,6 +48,14 @@ def step_flops(layers, batch):
     return sum(conv_flops(l, batch) * (2 if i == 0 else 3) for i, l in enumerate(layers))
 
 
+def max_over_ranks(torch, values, device="cuda"):
+    """Element-wise maximum of this rank's timings over all ranks (torch.distributed); the
+    whole-job time of a step is the slowest rank's."""
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -213,16 +221,6 @@ class Net:
                 d["dx32"] = None if d["first"] else torch.empty(batch, s.h, s.w, s.c, device=dev)
                 d["dw32"] = torch.empty(s.c * s.kh * s.kw * s.kn, device=dev)
 
-    def launches_bf16(self):
-        # fold, pack fwd (+ a K-padding fill when kh*kw*c8 is not a multiple of 64), fwd,
-        # [pack dgrad, dgrad], wgrad, wgrad reduce
-        n = 0
-        for d in self.L:
-            s = d["s"]
-            n += 5 if d["first"] else 7
-            n += 1 if (s.kh * s.kw * c8(s.c)) % 64 else 0
-        return n
-
     def launches_f32(self):
         return sum(3 if d["first"] else 4 for d in self.L)
 
@@ -280,7 +278,8 @@ def layer_bytes(l, batch, elem=2):
 
 
 def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
-    """CUDA-event time of each BF16 op of each layer (reps back to back), with its roofline bound."""
+    """Device time of each BF16 op of each layer (reps calls replayed from one CUDA graph),
+    with its roofline bound."""
     tc, cg = net.tc, net.cg
     rows = []
     pk_t = peaks["bf16_tflops_sustained"] * 1e12
@@ -296,15 +295,25 @@ def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
         row = {"layer": l["name"], "shape": [l["h"], l["c"], l["kn"], l["k"], l["stride"]], "gflop": fl / 1e9,
                "mb": by / 1e6, "roofline_us": max(fl / pk_t, by / pk_b) * 1e6}
         for name, fn in ops.items():
-            fn()
+            # `reps` calls captured in one CUDA graph: device time, not host launch cost
+            st = torch.cuda.Stream()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(st):
+                fn()
+                st.synchronize()
+                with torch.cuda.graph(g, stream=st):
+                    for _ in range(reps):
+                        fn()
+            torch.cuda.synchronize()
+            g.replay()
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
-            for _ in range(reps):
-                fn()
+            g.replay()
             b.record()
             torch.cuda.synchronize()
             us = a.elapsed_time(b) * 1000 / reps
+            del g
             row[name + "_us"] = us
             row[name + "_frac"] = row["roofline_us"] / us
         rows.append(row)
@@ -374,6 +383,431 @@ def grouped_cpu_baseline(specs, every=8, threads=None):
     return t_total, fl
 
 
+class VggNet:
+    """VGG-16 NCHW training step buffers (synthetic, seeded): the FP32 plain form on the
+    reference's NCHW layouts, and the BF16 form fed from the same FP32 NCHW tensors."""
+
+    def __init__(self, torch, cg, tc, layers, batch):
+        self.torch, self.cg, self.tc, self.layers, self.batch = torch, cg, tc, layers, batch
+        g = torch.Generator(device="cuda").manual_seed(20261204)
+        self.L = []
+        ws32 = ws16 = 16
+        for i, l in enumerate(layers):
+            s = cg.Shape.of(batch, l["h"], l["w"], l["c"], l["kn"], 3, 3, 1, 1, 1, 1, 1, 1)
+            K, kn = l["c"] * 9, l["kn"]
+            d = {"s": s, "first": i == 0}
+            d["x32"] = torch.randn(batch, l["c"], l["h"], l["w"], device="cuda", generator=g)
+            d["w32"] = torch.randn(kn, l["c"], 3, 3, device="cuda", generator=g) * (2.0 / K) ** 0.5   # OIHW
+            d["bias"] = torch.rand(kn, device="cuda", generator=g) * 0.2 - 0.1
+            d["dy32"] = torch.randn(batch, kn, l["h"], l["w"], device="cuda", generator=g) * 1e-2 ** 0.5
+            d["y32"] = torch.empty(batch, kn, l["h"], l["w"], device="cuda")
+            d["dx32"] = None if i == 0 else torch.empty(batch, l["c"], l["h"], l["w"], device="cuda")
+            d["dw32"] = torch.empty(kn, l["c"], 3, 3, device="cuda")
+            # BF16 form: NHWC BF16 activations, packed weights, FP32 dW in the NCHW API's OIHW layout
+            d["xb"] = torch.empty(batch, l["h"], l["w"], c8(l["c"]), device="cuda", dtype=torch.bfloat16)
+            d["dyb"] = torch.empty(batch, l["h"], l["w"], kn, device="cuda", dtype=torch.bfloat16)
+            d["yb"] = torch.empty(batch, l["h"], l["w"], kn, device="cuda", dtype=torch.bfloat16)
+            d["dxb"] = None if i == 0 else torch.empty(batch, l["h"], l["w"], l["c"], device="cuda",
+                                                       dtype=torch.bfloat16)
+            d["dwb"] = torch.empty(kn, l["c"], 3, 3, device="cuda")
+            d["wp"] = torch.empty(tc.weights_size(s, tc.OPERAND_FWD) // 2, device="cuda", dtype=torch.bfloat16)
+            d["wpd"] = None if i == 0 else torch.empty(tc.weights_size(s, tc.OPERAND_DGRAD) // 2, device="cuda",
+                                                       dtype=torch.bfloat16)
+            d["scale"] = torch.ones(kn, device="cuda")
+            d["shift"] = torch.empty(kn, device="cuda")
+            ws32 = max(ws32, cg.wgrad_f32_workspace_size(s))
+            ws16 = max(ws16, tc.wgrad_bf16_workspace_size(s))
+            self.L.append(d)
+        self.ws32 = torch.empty(ws32 // 4 + 1, device="cuda")
+        self.ws16 = torch.empty(ws16 // 4 + 1, device="cuda")
+
+    def step_f32(self):
+        cg = self.cg
+        for d in self.L:
+            s = d["s"]
+            cg.fwd_f32(cg.NCHW, s, d["w32"], d["x32"], d["y32"], bias=d["bias"], relu=True)
+            if not d["first"]:
+                cg.dgrad_f32(cg.NCHW, s, d["w32"], d["dy32"], d["dx32"], accumulate=False)
+            cg.wgrad_f32(cg.NCHW, s, d["dy32"], d["x32"], d["dw32"], self.ws32)
+
+    def wgrad_f32(self):
+        for d in self.L:
+            self.cg.wgrad_f32(self.cg.NCHW, d["s"], d["dy32"], d["x32"], d["dw32"], self.ws32)
+
+    def step_bf16(self):
+        cg, tc = self.cg, self.tc
+        for d in self.L:
+            s = d["s"]
+            tc.to_bf16_nhwc(cg.NCHW, s.b, s.c, s.h, s.w, d["x32"], d["xb"])
+            tc.to_bf16_nhwc(cg.NCHW, s.b, s.kn, s.h, s.w, d["dy32"], d["dyb"])
+            tc.fold_epilogue(s.kn, d["scale"], d["shift"], bias=d["bias"])
+            tc.pack_weights(cg.NCHW, s, tc.OPERAND_FWD, d["w32"], d["wp"])
+            tc.fwd_bf16(s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=True)
+            if not d["first"]:
+                tc.pack_weights(cg.NCHW, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
+                tc.dgrad_bf16(s, d["dyb"], d["wpd"], d["dxb"])
+            tc.wgrad_bf16(cg.NCHW, s, d["dyb"], d["xb"], d["dwb"], self.ws16)
+
+    def wgrad_bf16(self):
+        for d in self.L:
+            self.tc.wgrad_bf16(self.cg.NCHW, d["s"], d["dyb"], d["xb"], d["dwb"], self.ws16)
+
+
+def vgg_points_check(torch, O, net, idx_layers, npts=512):
+    """Max normwise relative error of y, dx, dW (FP32 and BF16 forms) against FP64 at sampled points."""
+    import numpy as np
+    rng = np.random.default_rng(5)
+    out = {}
+    for i in idx_layers:
+        d, l = net.L[i], net.layers[i]
+        s = d["s"]
+        g = dict(b=s.b, h=s.h, w=s.w, c=s.c, kn=s.kn, kh=3, kw=3, vpad=1, hpad=1, vstr=1, hstr=1, vdil=1, hdil=1)
+        x = d["x32"].cpu().numpy().ravel()
+        w = d["w32"].cpu().numpy().ravel()
+        dy = d["dy32"].cpu().numpy().ravel()
+        epi = {"bias": d["bias"].cpu().numpy(), "relu": True}
+        r = {}
+        # forward: NCHW points (b, k, y, x)
+        pb, pk, py, px = (rng.integers(0, n, npts) for n in (s.b, s.kn, s.h, s.w))
+        idx = ((pb * s.kn + pk) * s.h + py) * s.w + px
+        ref = O.fwd_points_f64(O.NCHW, g, w, x, idx, epi)
+        got32 = d["y32"].cpu().numpy().ravel()[idx]
+        gotb = d["yb"].float().cpu().numpy()[pb, py, px, pk]
+        scale = np.abs(ref).max() or 1.0
+        r["fwd"] = {"f32": float(np.abs(got32 - ref).max() / scale), "bf16": float(np.abs(gotb - ref).max() / scale)}
+        if not d["first"]:
+            pc = rng.integers(0, s.c, npts)
+            idx = ((pb * s.c + pc) * s.h + py) * s.w + px
+            ref = O.dgrad_points_f64(O.NCHW, g, w, dy, idx)
+            got32 = d["dx32"].cpu().numpy().ravel()[idx]
+            gotb = d["dxb"].float().cpu().numpy()[pb, py, px, pc]
+            scale = np.abs(ref).max() or 1.0
+            r["dgrad"] = {"f32": float(np.abs(got32 - ref).max() / scale),
+                          "bf16": float(np.abs(gotb - ref).max() / scale)}
+        idx = rng.integers(0, s.kn * s.c * 9, npts)
+        ref = O.wgrad_points_f64(O.NCHW, g, dy, x, idx)
+        scale = np.abs(ref).max() or 1.0
+        r["wgrad"] = {"f32": float(np.abs(d["dw32"].cpu().numpy().ravel()[idx] - ref).max() / scale),
+                      "bf16": float(np.abs(d["dwb"].cpu().numpy().ravel()[idx] - ref).max() / scale)}
+        out[l["name"]] = r
+    return out
+
+
+def vgg_cpu_baseline(layers, images, threads=None):
+    """The oracle port (FP32 NCHW, the reference's order) on `images` images through the 13 layers:
+    forward with bias + ReLU, input gradient (not layer 1), weight gradient.  Returns seconds."""
+    import numpy as np
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    rng = np.random.default_rng(3)
+    t = 0.0
+    for i, l in enumerate(layers):
+        g = dict(b=images, h=l["h"], w=l["w"], c=l["c"], kn=l["kn"], kh=3, kw=3, vpad=1, hpad=1, vstr=1, hstr=1,
+                 vdil=1, hdil=1)
+        K = l["c"] * 9
+        x = rng.standard_normal(images * l["c"] * l["h"] * l["w"]).astype(np.float32)
+        w = (rng.standard_normal(K * l["kn"]) * np.sqrt(2.0 / K)).astype(np.float32)
+        dy = (rng.standard_normal(images * l["kn"] * l["h"] * l["w"]) * 0.1).astype(np.float32)
+        y = np.empty(images * l["kn"] * l["h"] * l["w"], np.float32)
+        dw = np.empty(K * l["kn"], np.float32)
+        dx = np.zeros_like(x)
+        epi = {"bias": rng.uniform(-.1, .1, l["kn"]).astype(np.float32), "relu": True}
+        t0 = time.perf_counter()
+        O.call_fwd("port", O.NCHW, g, w, x, y, epi)
+        if i > 0:
+            O.call_back("port", O.NCHW, g, w, dy, dx)
+        O.call_fwd("port", O.NCHW, g, dy, x, dw, None, trans="T")
+        t += time.perf_counter() - t0
+    return t
+
+
+def run_vgg(args):
+    """VGG-16 NCHW training step (13 3x3 convs, batch 32): forward (bias + ReLU), input gradient,
+    split-K weight gradient, in the FP32 plain form and the BF16 tensor-core form."""
+    import torch
+    import convgemm_gb300 as cg
+    from convgemm_gb300 import tc
+    from convgemm_gb300.workloads import vgg16_layers
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cg.lib()
+    layers = vgg16_layers()
+    batch = 32 if args.batch == BATCH else args.batch
+    net = VggNet(torch, cg, tc, layers, batch)
+    flops = sum(conv_flops(l, batch) * (2 if i == 0 else 3) for i, l in enumerate(layers))
+    net.step_bf16()
+    net.step_f32()
+    torch.cuda.synchronize()
+    cg.check_device()
+
+    stream = torch.cuda.Stream()
+    graphs = {}
+    per_step = {}
+    for name, fn in (("bf16", net.step_bf16), ("f32", net.step_f32)):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            fn()
+            stream.synchronize()
+            n0 = cg.launch_count()
+            with torch.cuda.graph(g, stream=stream):
+                fn()
+            per_step[name] = cg.launch_count() - n0
+        graphs[name] = g
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    ms = timed(torch, graphs["bf16"].replay, args.steps, args.warmup, torch.cuda.current_stream())
+    clk = clocks.stop()
+    ms32 = timed(torch, graphs["f32"].replay, max(2, args.fp32_steps), 1, torch.cuda.current_stream())
+    if world > 1:
+        ms, ms32 = max_over_ranks(torch, [ms, ms32])
+    cg.check_device()
+
+    # dW bit-reproducibility run to run (both forms), then FP64 point checks
+    dw1 = [(d["dw32"].clone(), d["dwb"].clone()) for d in net.L]
+    net.wgrad_f32()
+    net.wgrad_bf16()
+    torch.cuda.synchronize()
+    repro = {"f32": all(torch.equal(a, d["dw32"]) for (a, _), d in zip(dw1, net.L)),
+             "bf16": all(torch.equal(b, d["dwb"]) for (_, b), d in zip(dw1, net.L))}
+    checks = None
+    if rank == 0:
+        from oracle import oracle as O
+        O.build(with_ref=False)
+        checks = vgg_points_check(torch, O, net, [0, 6, 12])
+
+    # e2e: the BF16 step through the API with the image batch and the top gradient from pinned
+    # host memory and every dW back to pinned host memory
+    img_h = torch.randn(batch, 3, 224, 224).pin_memory()
+    top_h = (torch.randn(batch, 512, 14, 14) * 0.1).pin_memory()
+    dw_h = [torch.empty(d["dwb"].shape).pin_memory() for d in net.L]
+    h2d = (img_h.numel() + top_h.numel()) * 4
+    d2h = sum(t.numel() * 4 for t in dw_h)
+
+    def e2e_step():
+        net.L[0]["x32"].copy_(img_h, non_blocking=True)
+        net.L[-1]["dy32"].copy_(top_h, non_blocking=True)
+        net.step_bf16()
+        for d, h in zip(net.L, dw_h):
+            h.copy_(d["dwb"], non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n_e2e = max(3, args.steps // 2)
+    for _ in range(n_e2e):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1000 / n_e2e
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t = vgg_cpu_baseline(layers, 1, os.cpu_count())
+        cpu = {"value": 1.0 / t, "unit": "img/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "1 image x 13 layers fwd + dX + dW, NCHW FP32, sconvGemmNCHW/_back of the oracle port"}
+    peaks, peak_kind = read_peaks()
+    tf = flops / (ms / 1000) / 1e12
+    if rank == 0:
+        line = {"metric": "VGG-16 NCHW conv training step img/s (fwd + dX + dW), BF16-TC and FP32 plain",
+                "value": world * batch / (ms / 1000), "unit": "img/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+                "config": {"workload": "vgg16: 13 3x3/s1/p1 convs at 224x224, fwd (bias + ReLU) + dX (not layer 1) "
+                                       "+ dW, NCHW FP32 tensors; the BF16 form converts x and dY to NHWC BF16 and "
+                                       "packs OIHW weights inside the step, dW in OIHW FP32",
+                           "global_batch": batch * world, "per_gpu_batch": batch, "seq_len": None,
+                           "parallelism": f"replicas{world}", "l2": "inputs larger than L2",
+                           "gflop_per_img": flops / batch / 1e9},
+                "tflops": tf,
+                "fp32_plain": {"value": world * batch / (ms32 / 1000), "unit": "img/s", "ms_per_step": ms32,
+                               "tflops": flops / (ms32 / 1000) / 1e12},
+                "bf16_vs_fp32": ms32 / ms,
+                "dw_bitwise_reproducible": repro, "fp64_point_errors": checks,
+                "roofline": {"bound": "tensor", "kernel": "whole BF16 step", "achieved": tf,
+                             "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                             "frac": tf / peaks["bf16_tflops_sustained"], "traffic": None,
+                             "peak_source": f"{peak_kind} bf16_tflops_sustained"},
+                "cpu_baseline": cpu,
+                "e2e": {"value": world * batch / (e2e_ms / 1000), "unit": "img/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "clocks": clk, "gpu_launches": per_step["bf16"] * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_forms(args):
+    """Forward pass of the 53 ResNet-50 convolutions at batch 128 in the three tensor-core
+    forms: BF16, FP8-E4M3 (per-tensor activation scale, per-channel weight scales, FP32
+    accumulation) and 3xBF16 (split products, FP32 output).  Each form's forward over all
+    layers is one CUDA graph; errors are max / RMS relative (normwise) against FP64 at
+    sampled output points of image 0 of every layer."""
+    import numpy as np
+    import torch
+    import convgemm_gb300 as cg
+    from convgemm_gb300 import tc
+    from oracle import oracle as O
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cg.lib()
+    if rank == 0:
+        O.build(with_ref=False)
+    layers = resnet50_layers()
+    batch = 128 if args.batch == BATCH else args.batch
+    gen = torch.Generator(device="cuda").manual_seed(20261205)
+    L = []
+    for i, l in enumerate(layers):
+        s = cg.Shape.of(batch, l["h"], l["w"], l["c"], l["kn"], l["k"], l["k"], l["pad"], l["pad"], l["stride"],
+                        l["stride"], 1, 1)
+        K, kn = l["c"] * l["k"] * l["k"], l["kn"]
+        d = {"s": s, "l": l, "relu": not (l["name"].endswith("conv3") or l["name"].endswith("down"))}
+        d["x"] = torch.randn(batch, l["h"], l["w"], l["c"], device="cuda", generator=gen)
+        d["w"] = torch.randn(K * kn, device="cuda", generator=gen) * (2.0 / K) ** 0.5
+        var = torch.rand(kn, device="cuda", generator=gen) * 1.5 + 0.5
+        d["epi"] = {"mean": torch.randn(kn, device="cuda", generator=gen) * 0.1,
+                    "inv_std": 1.0 / torch.sqrt(var + 1e-5),
+                    "gamma": torch.rand(kn, device="cuda", generator=gen) + 0.5,
+                    "beta": torch.rand(kn, device="cuda", generator=gen) * 0.2 - 0.1}
+        d["scale"], d["shift"] = torch.empty(kn, device="cuda"), torch.empty(kn, device="cuda")
+        tc.fold_epilogue(kn, d["scale"], d["shift"], **d["epi"])
+        # BF16
+        d["xb"] = torch.empty(batch, l["h"], l["w"], c8(l["c"]), device="cuda", dtype=torch.bfloat16)
+        tc.to_bf16_nhwc(cg.NHWC, batch, l["c"], l["h"], l["w"], d["x"], d["xb"])
+        d["wp"] = torch.empty(tc.weights_size(s, tc.OPERAND_FWD) // 2, device="cuda", dtype=torch.bfloat16)
+        tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, d["w"], d["wp"])
+        d["yb"] = torch.empty(batch, s.ho, s.wo, kn, device="cuda", dtype=torch.bfloat16)
+        d["fp8"] = l["c"] % 64 == 0   # FP8 / 3xBF16 forms need channels a multiple of 64 (not the stem)
+        if d["fp8"]:
+            d["xq"] = torch.empty(d["x"].numel(), dtype=torch.uint8, device="cuda")
+            d["xs"] = torch.zeros(2, device="cuda")
+            tc.fp8_quantize(d["x"], d["xq"], d["xs"])
+            d["wq"] = torch.empty(tc.fp8_weights_size(s), dtype=torch.uint8, device="cuda")
+            d["wsc"] = torch.empty(kn, device="cuda")
+            tc.fp8_pack_weights(cg.NHWC, s, d["w"], d["wq"], d["wsc"])
+            d["sc8"], d["sh8"] = torch.empty(kn, device="cuda"), torch.empty(kn, device="cuda")
+            tc.fp8_epilogue_scales(kn, d["scale"], d["shift"], d["wsc"], d["xs"], d["sc8"], d["sh8"])
+            d["y8"] = torch.empty(batch, s.ho, s.wo, kn, device="cuda", dtype=torch.bfloat16)
+            d["xh"] = torch.empty(d["x"].numel(), dtype=torch.bfloat16, device="cuda")
+            d["xl"] = torch.empty_like(d["xh"])
+            tc.split_bf16x2(d["x"], d["xh"], d["xl"])
+            d["wh"] = torch.empty(d["wp"].numel(), dtype=torch.bfloat16, device="cuda")
+            d["wl"] = torch.empty_like(d["wh"])
+            tc.bf16x3_pack_weights(cg.NHWC, s, d["w"], d["wh"], d["wl"])
+            d["y3"] = torch.empty(batch, s.ho, s.wo, kn, device="cuda")
+        L.append(d)
+    torch.cuda.synchronize()
+    cg.check_device()
+
+    def fwd(form):
+        def run():
+            for d in L:
+                s = d["s"]
+                if form == "bf16" or not d["fp8"]:
+                    if form == "bf16":
+                        tc.fwd_bf16(s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=d["relu"])
+                elif form == "fp8":
+                    tc.fwd_fp8(s, d["xq"], d["wq"], d["y8"], d["sc8"], d["sh8"], relu=d["relu"])
+                else:
+                    tc.fwd_bf16x3(s, d["xh"], d["xl"], d["wh"], d["wl"], d["y3"], d["scale"], d["shift"],
+                                  relu=d["relu"])
+        return run
+
+    peaks, peak_kind = read_peaks()
+    stream = torch.cuda.Stream()
+    res = {}
+    clk = None
+    for form in ("bf16", "fp8", "bf16x3"):
+        fn = fwd(form)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(stream):
+            fn()
+            stream.synchronize()
+            n0 = cg.launch_count()
+            with torch.cuda.graph(g, stream=stream):
+                fn()
+            nl = cg.launch_count() - n0
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local) if form == "fp8" else None
+        ms = timed(torch, g.replay, args.steps, args.warmup, torch.cuda.current_stream())
+        if clocks:
+            clk = clocks.stop()
+        if world > 1:
+            ms = max_over_ranks(torch, [ms])[0]
+        cg.check_device()
+        fl = sum(conv_flops(d["l"], batch) for d in L if form == "bf16" or d["fp8"])
+        issued = fl * (3 if form == "bf16x3" else 1)
+        peak = peaks["bf16_tflops"] * (2 if form == "fp8" else 1)
+        res[form] = {"ms": ms, "gflop": fl / 1e9, "tflops": fl / (ms / 1000) / 1e12,
+                     "issued_tflops": issued / (ms / 1000) / 1e12, "launches": nl,
+                     "tensor_frac": issued / (ms / 1000) / 1e12 / peak,
+                     "layers": sum(1 for d in L if form == "bf16" or d["fp8"])}
+        del g
+
+    # errors against FP64 at sampled points of image 0
+    if rank == 0:
+        rng = np.random.default_rng(9)
+        errs = {"bf16": [], "fp8": [], "bf16x3": []}
+        for d in L:
+            s, l = d["s"], d["l"]
+            g1 = dict(b=1, h=s.h, w=s.w, c=s.c, kn=s.kn, kh=s.kh, kw=s.kw, vpad=s.vpad, hpad=s.hpad,
+                      vstr=s.vstride, hstr=s.hstride, vdil=1, hdil=1)
+            x0 = d["x"][0].contiguous().cpu().numpy().ravel()
+            w = d["w"].cpu().numpy()
+            epi = {k: v.cpu().numpy() for k, v in d["epi"].items()}
+            epi["relu"] = d["relu"]
+            npts = 1024
+            py, px, pk = rng.integers(0, s.ho, npts), rng.integers(0, s.wo, npts), rng.integers(0, s.kn, npts)
+            idx = (py * s.wo + px) * s.kn + pk
+            ref = O.fwd_points_f64(O.NHWC, g1, w, x0, idx, epi)
+            outs = {"bf16": d["yb"][0].float().cpu().numpy().ravel()[idx]}
+            if d["fp8"]:
+                outs["fp8"] = d["y8"][0].float().cpu().numpy().ravel()[idx]
+                outs["bf16x3"] = d["y3"][0].cpu().numpy().ravel()[idx]
+            for f, o in outs.items():
+                dd = o - ref
+                errs[f].append((float(np.abs(dd).max() / max(np.abs(ref).max(), 1e-300)),
+                                float(np.sqrt(np.mean(dd * dd)) / max(np.sqrt(np.mean(ref * ref)), 1e-300)),
+                                l["name"]))
+        for f, e in errs.items():
+            worst = max(e)
+            res[f].update({"max_rel_err": worst[0], "max_rel_err_layer": worst[2],
+                           "rms_rel_err": max(v[1] for v in e)})
+        line = {"metric": "ResNet-50 layer set forward at batch 128: TFLOP/s and error of the FP8-E4M3 and "
+                          "3xBF16 forms beside BF16",
+                "value": res["fp8"]["tflops"], "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": res["fp8"]["ms"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "e4m3", "data": "synthetic",
+                "config": {"workload": "resnet50 v1.5 53 convs forward (folded BN + ReLU), batch 128, NHWC; FP8 and "
+                                       "3xBF16 on the 52 layers with channels a multiple of 64 (the stem stays BF16 "
+                                       "and is not counted in their lines)",
+                           "global_batch": batch * world, "parallelism": f"replicas{world}",
+                           "l2": "inputs larger than L2"},
+                "forms": res,
+                "roofline": {"bound": "tensor", "kernel": "tc_conv_kernel (FP8 forward)",
+                             "achieved": res["fp8"]["tflops"], "peak": peaks["bf16_tflops"] * 2,
+                             "unit": "TFLOP/s", "frac": res["fp8"]["tensor_frac"], "traffic": None,
+                             "peak_source": f"2 x {peak_kind} bf16_tflops (the nominal FP8:BF16 dense ratio)"},
+                "errors_how": "normwise max|d|/max|ref| and RMS(d)/RMS(ref) against the FP64 direct convolution of "
+                              "the FP32 inputs at 1024 sampled outputs of image 0 of every layer; worst layer",
+                "cpu_baseline": None, "e2e": None, "clocks": clk,
+                "gpu_launches": res["fp8"]["launches"] * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def run_grouped(args):
     """256 independent uneven BF16 convolutions (bias + ReLU): one persistent grouped launch
     in a CUDA graph, against one launch per convolution (also in a CUDA graph)."""
@@ -425,14 +859,17 @@ def run_grouped(args):
 
     stream = torch.cuda.Stream()
     graphs = {}
+    per_step = {}
     for name, fn in (("grouped", grp.launch), ("grouped_default_widths", default_grp.launch),
                      ("per_conv", per_conv)):
         with torch.cuda.stream(stream):
             fn()
             stream.synchronize()
             g = torch.cuda.CUDAGraph()
+            n0 = cg.launch_count()
             with torch.cuda.graph(g, stream=stream):
                 fn()
+            per_step[name] = cg.launch_count() - n0
         graphs[name] = g
     torch.cuda.synchronize()
     cg.check_device()
@@ -447,9 +884,7 @@ def run_grouped(args):
         times[name] = timed(torch, graphs[name].replay, args.steps, args.warmup, torch.cuda.current_stream())
     times["per_conv_eager"] = timed(torch, per_conv, max(3, args.steps // 2), 1, torch.cuda.current_stream())
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(torch, [ms])[0]
     cg.check_device()
     value = world * flops / (ms / 1000) / 1e12
 
@@ -495,7 +930,8 @@ def run_grouped(args):
                 "max_rel_diff_vs_per_conv": diff, "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": world * flops / (e2e_ms / 1000) / 1e12, "unit": "TFLOP/s",
                         "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms},
-                "clocks": clk, "gpu_launches": args.steps}
+                "clocks": clk, "gpu_launches": per_step["grouped"] * args.steps,
+                "per_conv_launches_per_step": per_step["per_conv"]}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -517,7 +953,7 @@ def main():
     ap.add_argument("--only", default=None,
                     help="LAYER:OP (e.g. s3b2_conv2:fwd): run just that BF16 op, eagerly, warmup+steps times "
                          "(for profiler captures)")
-    ap.add_argument("--workload", default="resnet50", choices=["resnet50", "grouped"],
+    ap.add_argument("--workload", default="resnet50", choices=["resnet50", "grouped", "vgg16", "forms"],
                     help="resnet50: the headline fwd+bwd step; grouped: uneven convolutions in one launch")
     ap.add_argument("--group-n", type=int, default=256)
     args = ap.parse_args()
@@ -526,6 +962,10 @@ def main():
         return run_reference(args)
     if args.workload == "grouped":
         return run_grouped(args)
+    if args.workload == "vgg16":
+        return run_vgg(args)
+    if args.workload == "forms":
+        return run_forms(args)
 
     import torch
     import convgemm_gb300 as cg
@@ -557,8 +997,10 @@ def main():
     with torch.cuda.stream(stream):
         net.step_bf16()
         torch.cuda.synchronize()
+        n0 = cg.launch_count()
         with torch.cuda.graph(graph, stream=stream):
             net.step_bf16()
+        launches_per_step = cg.launch_count() - n0
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -566,9 +1008,7 @@ def main():
     ms = timed(torch, graph.replay, args.steps, args.warmup, torch.cuda.current_stream())
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(torch, [ms])[0]
     cg.check_device()
     value = world * batch / (ms / 1000.0)
 
@@ -578,8 +1018,10 @@ def main():
     for fam in ("prep", "fwd", "dgrad", "wgrad"):
         g_f = torch.cuda.CUDAGraph()
         with torch.cuda.stream(stream):
+            n0 = cg.launch_count()
             with torch.cuda.graph(g_f, stream=stream):
-                n_launch = net.step_family(fam)
+                net.step_family(fam)
+            n_launch = cg.launch_count() - n0
         torch.cuda.synchronize()
         ms_f = timed(torch, g_f.replay, max(5, args.steps), 2, torch.cuda.current_stream())
         fl = net.family_flops(fam)
@@ -663,7 +1105,8 @@ def main():
                 "tflops": flops / (ms / 1000) / 1e12,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "fp32_plain": fp32,
                 "bf16_vs_fp32": (value / fp32["value"]) if fp32 else None,
-                "clocks": clk, "gpu_launches": net.launches_bf16() * args.steps}
+                "clocks": clk, "gpu_launches": launches_per_step * args.steps,
+                "gpu_launches_how": "library launch counter (convgemm_launch_count) across the capture of one step, x steps"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -115,6 +115,7 @@ def lib():
         L.convgemm_split_bf16x2.argtypes = [ctypes.c_size_t, _VP, _VP, _VP, _VP]
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
+        L.convgemm_launch_count.restype = ctypes.c_ulonglong
         L.convgemm_group_weights_size.argtypes = [SP]
         L.convgemm_group_weights_size.restype = ctypes.c_size_t
         L.convgemm_group_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP]
@@ -124,6 +125,11 @@ def lib():
         L.convgemm_group_launch.argtypes = [_VP, _I, _I, _VP]
         _lib = L
     return _lib
+
+
+def launch_count() -> int:
+    """Kernels launched (or captured) by the library so far in this process."""
+    return int(lib().convgemm_launch_count())
 
 
 def last_error() -> tuple[int, str]:

@@ -403,7 +403,7 @@ cudaError_t launch(const Op &op, int gz, cudaStream_t st) {
     }
     dim3 grid((op.M() + BM - 1) / BM, (op.N() + BN - 1) / BN, gz);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    fp32_igemm_kernel<Op><<<grid, NT, S_SMEM_BYTES, st>>>(op);
+    fp32_igemm_kernel<Op><<<grid, NT, S_SMEM_BYTES, st>>>(op); cg_note_launch();
     return cudaGetLastError();
 }
 
@@ -449,7 +449,7 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     if (e != cudaSuccess) return e;
     const long long total = (long long) op.g.K * op.g.kn;
     int blocks = (int) std::min<long long>((total + 255) / 256, 152LL * 16);
-    wgrad_reduce_kernel<<<blocks, 256, 0, st>>>(ws, dw, op.g.K, op.g.kn, nblocks, nchw);
+    wgrad_reduce_kernel<<<blocks, 256, 0, st>>>(ws, dw, op.g.K, op.g.kn, nblocks, nchw); cg_note_launch();
     return cudaGetLastError();
 }
 

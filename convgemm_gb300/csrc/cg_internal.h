@@ -35,3 +35,5 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
 
 // Device error word (set by bounded waits); defined in cg_runtime.cu.
 int *cg_device_error_word();
+// Counts one kernel launch made by the library (convgemm_launch_count).
+void cg_note_launch();

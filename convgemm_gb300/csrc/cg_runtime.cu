@@ -1,6 +1,7 @@
 // Host runtime of the library: the C ABI of convGemm.h and convgemm_gpu.h,
 // argument checks, error reporting, host-pointer staging and the cached
 // device buffers the void drop-in entry points need.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,10 @@ convgemm_status_t cg_cuda_check(cudaError_t e, const char *what) {
     return cg_set_error(e == cudaErrorMemoryAllocation ? CONVGEMM_ERROR_ALLOC : CONVGEMM_ERROR_CUDA,
                         "%s: %s", what, cudaGetErrorString(e));
 }
+
+static std::atomic<unsigned long long> g_launches{0};
+void cg_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" unsigned long long convgemm_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 extern "C" convgemm_status_t convgemm_get_last_status(void) { return tl_status; }
 extern "C" const char *convgemm_get_last_error(void) { return tl_msg; }

@@ -214,34 +214,34 @@ cudaError_t prep_pack_fwd(const float *w, int nchw, int C, int kh, int kw, int k
                           cudaStream_t st) {
     if (nchw) {
         pack_fwd_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad,
-                                                                        (bf16 *) out);
+                                                                        (bf16 *) out); cg_note_launch();
         return cudaGetLastError();
     }
     const int khw = kh * kw;
     dim3 grid((Cp + 31) / 32, (kn + 31) / 32, khw), block(32, 8);
-    pack_fwd_tiled_kernel<<<grid, block, 0, st>>>(w, C, khw, kn, Cp, Kpad, (bf16 *) out);
+    pack_fwd_tiled_kernel<<<grid, block, 0, st>>>(w, C, khw, kn, Cp, Kpad, (bf16 *) out); cg_note_launch();
     if (Kpad > khw * Cp)
         pack_fwd_tail_kernel<<<grid_for((long long) kn * (Kpad - khw * Cp)), 256, 0, st>>>(kn, khw * Cp, Kpad,
-                                                                                          (bf16 *) out);
+                                                                                          (bf16 *) out); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_pack_dgrad(const float *w, int nchw, int C, int kh, int kw, int kn, int knp,
                             const PackDgradInfo &info, void *out, cudaStream_t st) {
     pack_dgrad_kernel<<<grid_for((long long) C * info.Ktot), 256, 0, st>>>(w, nchw, C, kh, kw, kn, knp, info,
-                                                                          (bf16 *) out);
+                                                                          (bf16 *) out); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_fold(int kn, const float *bias, const float *mean, const float *inv_std, const float *gamma,
                       const float *beta, float *scale, float *shift, cudaStream_t st) {
-    fold_kernel<<<(kn + 127) / 128, 128, 0, st>>>(kn, bias, mean, inv_std, gamma, beta, scale, shift);
+    fold_kernel<<<(kn + 127) / 128, 128, 0, st>>>(kn, bias, mean, inv_std, gamma, beta, scale, shift); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_to_bf16_nhwc(const float *in, int nchw, int B, int C, int H, int W, int Cp, void *out,
                               cudaStream_t st) {
-    to_bf16_nhwc_kernel<<<grid_for((long long) B * H * W * Cp), 256, 0, st>>>(in, nchw, B, C, H, W, Cp, (bf16 *) out);
+    to_bf16_nhwc_kernel<<<grid_for((long long) B * H * W * Cp), 256, 0, st>>>(in, nchw, B, C, H, W, Cp, (bf16 *) out); cg_note_launch();
     return cudaGetLastError();
 }
 
@@ -249,33 +249,33 @@ cudaError_t prep_fp8_quantize(long long n, int in_bf16, const void *in, void *ou
                               cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(amax_tmp, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    amax_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp);
-    quant_e4m3_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp, (uint8_t *) out, scale);
+    amax_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp); cg_note_launch();
+    quant_e4m3_kernel<<<grid_for(n), 256, 0, st>>>(in, in_bf16, n, amax_tmp, (uint8_t *) out, scale); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_pack_fp8(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *out,
                           float *wscale, cudaStream_t st) {
-    wscale_kernel<<<(kn + 127) / 128, 128, 0, st>>>(w, nchw, C * kh * kw, kn, wscale);
+    wscale_kernel<<<(kn + 127) / 128, 128, 0, st>>>(w, nchw, C * kh * kw, kn, wscale); cg_note_launch();
     pack_fp8_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, wscale,
-                                                                    (uint8_t *) out);
+                                                                    (uint8_t *) out); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_fp8_scales(int kn, const float *scale, const float *shift, const float *wscale, const float *xscale,
                             float *out_scale, float *out_shift, cudaStream_t st) {
-    fp8_scales_kernel<<<(kn + 127) / 128, 128, 0, st>>>(kn, scale, shift, wscale, xscale, out_scale, out_shift);
+    fp8_scales_kernel<<<(kn + 127) / 128, 128, 0, st>>>(kn, scale, shift, wscale, xscale, out_scale, out_shift); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_split(long long n, const float *in, void *hi, void *lo, cudaStream_t st) {
-    split_kernel<<<grid_for(n), 256, 0, st>>>(in, n, (bf16 *) hi, (bf16 *) lo);
+    split_kernel<<<grid_for(n), 256, 0, st>>>(in, n, (bf16 *) hi, (bf16 *) lo); cg_note_launch();
     return cudaGetLastError();
 }
 
 cudaError_t prep_pack_split(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *hi,
                             void *lo, cudaStream_t st) {
     pack_split_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, (bf16 *) hi,
-                                                                      (bf16 *) lo);
+                                                                      (bf16 *) lo); cg_note_launch();
     return cudaGetLastError();
 }

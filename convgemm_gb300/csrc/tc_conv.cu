@@ -30,6 +30,7 @@
 
 #include "cg_common.cuh"
 #include "tc_conv.h"
+#include "tc_epi.cuh"
 #include "tc_ptx.cuh"
 
 namespace {
@@ -361,37 +362,30 @@ __global__ void __launch_bounds__(288, 1)
                         if (p.relu) a = fmaxf(a, 0.0f);
                         pk[jj] = __float_as_uint(a);
                     }
+                } else if (p.relu) {
+                    tc::epi_bf16_64<true>(v0, v1, scp + c0, shp + c0, pk);
                 } else {
-#pragma unroll
-                    for (int jj = 0; jj < 32; jj++) {
-                        float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
-                        float b = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
-                        a = fmaf(a, scp[c0 + 2 * jj], shp[c0 + 2 * jj]);
-                        b = fmaf(b, scp[c0 + 2 * jj + 1], shp[c0 + 2 * jj + 1]);
-                        if (p.relu) {
-                            a = fmaxf(a, 0.0f);
-                            b = fmaxf(b, 0.0f);
-                        }
-                        pk[jj] = pack_bf16x2(a, b);
-                    }
+                    tc::epi_bf16_64<false>(v0, v1, scp + c0, shp + c0, pk);
                 }
                 if (p.epi_tma) {
-                    // 128-row chunk through shared memory, stored by TMA (out-of-range rows/columns clipped)
-                    if (et == 0) {
+                    // each warp stages its 32 rows (4 KB) and stores them with its own TMA
+                    // store: no barrier across the epilogue warps (out-of-range rows/columns
+                    // are clipped by the store)
+                    if (lane == 0) {
                         if (C::EPI_BUFS == 2) bulk_wait_read<1>();
                         else bulk_wait_read<0>();
                     }
-                    epi_bar();
-                    uint8_t *stg = epi_smem + ebuf * C::EPI_BYTES;
+                    __syncwarp();
+                    uint8_t *stg = epi_smem + ebuf * C::EPI_BYTES + ew * (C::EPI_BYTES / 4);
 #pragma unroll
                     for (int q = 0; q < 8; q++) {
                         uint4 u = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
-                        *reinterpret_cast<uint4 *>(stg + row * 128 + ((q ^ (row & 7)) << 4)) = u;
+                        *reinterpret_cast<uint4 *>(stg + lane * 128 + ((q ^ (lane & 7)) << 4)) = u;
                     }
                     tc::fence_proxy_async_smem();
-                    epi_bar();
-                    if (et == 0 && nb < p.Cout) {
-                        tma_store_2d(&omap, tc::smem_u32(stg), nb, tl.m0);
+                    __syncwarp();
+                    if (lane == 0 && nb < p.Cout && tl.m0 + ew * 32 < M) {
+                        tma_store_2d(&omap, tc::smem_u32(stg), nb, tl.m0 + ew * 32);
                         bulk_commit();
                     }
                     if (C::EPI_BUFS == 2) ebuf ^= 1;
@@ -417,7 +411,7 @@ __global__ void __launch_bounds__(288, 1)
                 }
             }
         }
-        if (et == 0) bulk_wait_all();
+        if (lane == 0) bulk_wait_all();
     } else {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
@@ -490,7 +484,7 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUte
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap, amaps);
+    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap, amaps); cg_note_launch();
     return cudaGetLastError();
 }
 

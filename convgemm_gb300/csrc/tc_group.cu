@@ -24,6 +24,7 @@
 #include "cg_common.cuh"
 #include "prep.h"
 #include "tc_host.h"
+#include "tc_epi.cuh"
 #include "tc_ptx.cuh"
 
 namespace {
@@ -33,7 +34,7 @@ using bf16 = __nv_bfloat16;
 struct alignas(64) GroupProblem {
     CUtensorMap amap;   // im2col map of x: 128 pixels x 64 channels per load
     CUtensorMap wmap;   // packed weights [kn][taps * c64]: box 64 x bn
-    CUtensorMap omap;   // y as [pixels][kn]: box 64 x 128
+    CUtensorMap omap;   // y as [pixels][kn]: box 64 x 32 (one epilogue warp's rows)
     int tile0, tile_end, count, ntiles_n, bn, M;   // count: convolutions in the table
     int ktiles, cpb, isy, isx, lo_y, lo_x, Cout, relu;
     uint32_t idesc;
@@ -47,7 +48,7 @@ constexpr int GSTAGES = 4;
 constexpr uint32_t A_BYTES = 128 * 128;
 constexpr uint32_t B_MAX = GBN * 128;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_MAX;
-constexpr uint32_t EPI_BYTES = 128 * 128;
+constexpr uint32_t EPI_BYTES = 128 * 128;   // one 64-column chunk of a tile (4 KB per epilogue warp)
 constexpr size_t GSMEM = 1024 + GSTAGES * STAGE_BYTES + EPI_BYTES + 256 + 2 * GBN * 4;
 static_assert(GSMEM <= 232448, "shared memory above the 227 KB per-block limit");
 
@@ -56,11 +57,6 @@ __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: 
 __device__ __forceinline__ int advance(const GroupProblem *probs, int nprob, int pi, int tile) {
     while (pi + 1 < nprob && tile >= __ldg(&probs[pi + 1].tile0)) pi++;
     return pi;
-}
-
-__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
-    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<uint32_t *>(&v);
 }
 
 __global__ void __launch_bounds__(288, 1)
@@ -150,7 +146,7 @@ __global__ void __launch_bounds__(288, 1)
             const GroupProblem *P = probs + pi;
             const int local = tile - __ldg(&P->tile0), ntn = __ldg(&P->ntiles_n), bn = __ldg(&P->bn);
             const int m0 = (local / ntn) * 128, n0 = (local % ntn) * bn;
-            const int Cout = __ldg(&P->Cout), relu = __ldg(&P->relu);
+            const int Cout = __ldg(&P->Cout), relu = __ldg(&P->relu), M = __ldg(&P->M);
             const float *scale = P->scale, *shift = P->shift;
             epi_bar();   // the previous tile's readers of the tables are done
             for (int jj = et; jj < bn; jj += 128) {
@@ -174,37 +170,31 @@ __global__ void __launch_bounds__(288, 1)
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
                 uint32_t pk[32];
-#pragma unroll
-                for (int jj = 0; jj < 32; jj++) {
-                    float a = __uint_as_float(jj < 16 ? v0[2 * jj] : v1[2 * jj - 32]);
-                    float bb = __uint_as_float(jj < 16 ? v0[2 * jj + 1] : v1[2 * jj + 1 - 32]);
-                    a = fmaf(a, sc_tab[c0 + 2 * jj], sh_tab[c0 + 2 * jj]);
-                    bb = fmaf(bb, sc_tab[c0 + 2 * jj + 1], sh_tab[c0 + 2 * jj + 1]);
-                    if (relu) {
-                        a = fmaxf(a, 0.0f);
-                        bb = fmaxf(bb, 0.0f);
-                    }
-                    pk[jj] = pack_bf16x2(a, bb);
-                }
-                if (et == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-                epi_bar();
+                if (relu)
+                    tc::epi_bf16_64<true>(v0, v1, sc_tab + c0, sh_tab + c0, pk);
+                else
+                    tc::epi_bf16_64<false>(v0, v1, sc_tab + c0, sh_tab + c0, pk);
+                // each warp stages its 32 rows and stores them itself: no barrier across warps
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                __syncwarp();
+                uint8_t *stg = epi + ew * (EPI_BYTES / 4);
 #pragma unroll
                 for (int qq = 0; qq < 8; qq++)
-                    *reinterpret_cast<uint4 *>(epi + row * 128 + ((qq ^ (row & 7)) << 4)) =
+                    *reinterpret_cast<uint4 *>(stg + lane * 128 + ((qq ^ (lane & 7)) << 4)) =
                         make_uint4(pk[4 * qq], pk[4 * qq + 1], pk[4 * qq + 2], pk[4 * qq + 3]);
                 tc::fence_proxy_async_smem();
-                epi_bar();
-                if (et == 0 && n0 + c0 < Cout) {
+                __syncwarp();
+                if (lane == 0 && n0 + c0 < Cout && m0 + ew * 32 < M) {
                     asm volatile(
                         "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
                             (uint64_t) &P->omap),
-                        "r"(tc::smem_u32(epi)), "r"(n0 + c0), "r"(m0)
+                        "r"(tc::smem_u32(stg)), "r"(n0 + c0), "r"(m0 + ew * 32)
                         : "memory");
                     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                 }
             }
         }
-        if (et == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     } else {
         // -------------------------------------------------- MMA issuer
         if (lane == 0) {
@@ -324,7 +314,7 @@ extern "C" convgemm_status_t convgemm_group_prepare(int n, const convgemm_group_
         if (convgemm_status_t e = tc_make_map_2d(&P.wmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, cv.w, s.kn,
                                                  s.kh * s.kw * c64, 64, bn))
             return e;
-        if (convgemm_status_t e = tc_make_map_2d(&P.omap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, cv.y, g.P, s.kn, 64, 128))
+        if (convgemm_status_t e = tc_make_map_2d(&P.omap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, cv.y, g.P, s.kn, 64, 32))
             return e;
         if (g.P > (1LL << 31) - 256 || (long long) s.b * s.h * s.w * c64 > (1LL << 31) - 1)
             return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: conv %d has more than 2^31 elements", fn, i);
@@ -374,6 +364,6 @@ extern "C" convgemm_status_t convgemm_group_launch(const void *table, int n, int
     }
     const int sms = tc_num_sms();
     const int grid = total_tiles < sms ? total_tiles : sms;
-    tc_group_kernel<<<grid, 288, GSMEM, (cudaStream_t) stream>>>((const GroupProblem *) table, n, total_tiles, err);
+    tc_group_kernel<<<grid, 288, GSMEM, (cudaStream_t) stream>>>((const GroupProblem *) table, n, total_tiles, err); cg_note_launch();
     return cg_cuda_check(cudaGetLastError(), "grouped kernel launch");
 }

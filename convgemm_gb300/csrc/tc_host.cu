@@ -298,7 +298,7 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
         const bool f32 = mode == 2;
         if (convgemm_status_t e = tc_make_map_2d(&omap, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
                                                  f32 ? 4 : 2, out, (long long) s.b * pl.Hout * pl.Wout, pl.Cout,
-                                                 f32 ? 32 : 64, 128))
+                                                 f32 ? 32 : 64, 32))
             return e;
     }
     p.in = (const __nv_bfloat16 *) in;
@@ -502,7 +502,7 @@ WgPlan plan_wgrad(const cg_shape &s) {
     if (splits < 1) splits = 1;
     w.cps = (w.nchunks + splits - 1) / splits;
     w.splits = (w.nchunks + w.cps - 1) / w.cps;
-    w.ws_bytes = sizeof(float) * (size_t) w.splits * (size_t) w.Nx * (size_t) s.kn;
+    w.ws_bytes = sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
     return w;
 }
 
@@ -571,7 +571,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
         return e;
-    return cg_cuda_check(tc_wgrad_reduce((const float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
+    return cg_cuda_check(tc_wgrad_reduce((float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
                                          s.kw, layout == CONVGEMM_NCHW, st),
                          "weight-gradient reduction");
 }

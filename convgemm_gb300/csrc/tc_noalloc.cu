@@ -10,7 +10,8 @@
 //
 // Limits and sharing:
 //   * the scratch holds CONVGEMM_NOALLOC_SCRATCH_FLOATS FP32 values (16 MiB);
-//     the number of pixel splits is capped so splits*Nx*kn fits, and a layer
+//     the number of pixel splits is capped so the partials (and the group sums
+//     of the two-pass reduction) fit, and a layer
 //     whose single partial tile (Nx*kn, Nx = kh*kw*c8) does not fit is
 //     rejected with CONVGEMM_ERROR_NOT_SUPPORTED;
 //   * every GPU that loads the library holds the 16 MiB until the process exits;
@@ -109,8 +110,14 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
     const int fit = (int) ((long long) CONVGEMM_NOALLOC_SCRATCH_FLOATS / tile);
     if (splits > fit) splits = fit;
     if (splits < 1) splits = 1;
-    const int cps = (nchunks + splits - 1) / splits;
+    int cps = (nchunks + splits - 1) / splits;
     splits = (nchunks + cps - 1) / cps;
+    // the reduction's group planes follow the split planes in the scratch
+    while (splits > 1 && (long long) (splits + tc_wgrad_groups(splits)) * tile > (long long) CONVGEMM_NOALLOC_SCRATCH_FLOATS) {
+        splits--;
+        cps = (nchunks + splits - 1) / splits;
+        splits = (nchunks + cps - 1) / cps;
+    }
 
     CUtensorMap map;
     if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, kn8, 64, 64)) return e;

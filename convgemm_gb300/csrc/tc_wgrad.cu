@@ -4,8 +4,9 @@
 // whose reduction runs over all b*ho*wo output pixels.  The pixels are cut
 // into 64-pixel chunks and the chunks into `splits` contiguous ranges, one per
 // blockIdx.z; each CTA writes its FP32 partial tile to a workspace and
-// wgrad_reduce adds the splits in increasing order, so the result is
-// bit-reproducible run to run (no float atomics).
+// the reduction adds the splits in a fixed order (in increasing split order,
+// or, with many splits, in fixed contiguous groups whose sums are then added in
+// group order), so the result is bit-reproducible run to run (no float atomics).
 //
 // Both operands reach the tensor core MN-major (the pixel index is the slow,
 // K dimension in memory):
@@ -242,6 +243,27 @@ __global__ void __launch_bounds__(160, 1)
     if (warp == 4) tc::tmem_dealloc(tmem, BN);
 }
 
+// First pass of the reduction when there are many splits: group g sums the
+// splits [g*per, min((g+1)*per, splits)) in split order into gs[g].  The
+// grouping depends only on the split count, so results stay bit-reproducible.
+__global__ void wgrad_group_sum_kernel(const float *__restrict__ ws, float *__restrict__ gs, int splits, int per,
+                                       size_t plane) {
+    const size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
+    if (i >= plane) return;
+    const int z0 = blockIdx.y * per, z1 = min(splits, z0 + per);
+    float s = ws[(size_t) z0 * plane + i];
+    int z = z0 + 1;
+    for (; z + 8 <= z1; z += 8) {
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = ws[(size_t) (z + j) * plane + i];
+#pragma unroll
+        for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
+    }
+    for (; z < z1; z++) s = __fadd_rn(s, ws[(size_t) z * plane + i]);
+    gs[(size_t) blockIdx.y * plane + i] = s;
+}
+
 // dW = sum over splits in increasing order, written in the requested layout:
 //   layout 0 (NHWC API): [ci][kh][kw][co];  layout 1 (NCHW API): [co][ci][kh][kw].
 // 32 x 32 tiles of (co, n = tap*Cp + ci): the split partials are read along their
@@ -273,11 +295,11 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
             for (; z + 8 <= splits; z += 8) {
                 float v[8];
 #pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = ws[(z + j) * plane + off];
+                for (int j = 0; j < 8; j++) v[j] = ws[(size_t) (z + j) * plane + off];
 #pragma unroll
                 for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
             }
-            for (; z < splits; z++) s = __fadd_rn(s, ws[z * plane + off]);
+            for (; z < splits; z++) s = __fadd_rn(s, ws[(size_t) z * plane + off]);
         }
         if (xa) tile[tx][r] = s;   // tile[co][n]
         else tile[r][tx] = s;
@@ -312,7 +334,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, 160, C::SMEM, st>>>(p, map, xmap);
+    kern<<<grid, 160, C::SMEM, st>>>(p, map, xmap); cg_note_launch();
     return cudaGetLastError();
 }
 
@@ -343,9 +365,29 @@ cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, co
                     : launch_wg_any<false>(p, dymap, xmap, bn, xa, grid, st);
 }
 
-cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
-                            int kw, int layout, cudaStream_t st) {
+int tc_wgrad_groups(int splits) {
+    if (splits <= 16) return 0;
+    int g = splits / 8;   // about eight splits per group
+    if (g > 32) g = 32;
+    const int per = (splits + g - 1) / g;
+    return (splits + per - 1) / per;   // every group non-empty
+}
+
+cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh, int kw,
+                            int layout, cudaStream_t st) {
+    const size_t plane = (size_t) Nx * kn;
+    const int groups = tc_wgrad_groups(splits);
+    const float *src = ws;
+    int n = splits;
+    if (groups) {
+        float *gs = ws + (size_t) splits * plane;
+        const int per = (splits + groups - 1) / groups;
+        dim3 g1((unsigned) ((plane + 255) / 256), groups);
+        wgrad_group_sum_kernel<<<g1, 256, 0, st>>>(ws, gs, splits, per, plane); cg_note_launch();
+        src = gs;
+        n = groups;
+    }
     dim3 grid((kn + 31) / 32, (Nx + 31) / 32), block(32, 8);
-    wgrad_reduce_kernel<<<grid, block, 0, st>>>(ws, dw, splits, xa, Nx, kn, C, Cp, kh * kw, layout);
+    wgrad_reduce_kernel<<<grid, block, 0, st>>>(src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout); cg_note_launch();
     return cudaGetLastError();
 }

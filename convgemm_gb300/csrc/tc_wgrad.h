@@ -19,5 +19,10 @@ struct TcWgradParams {
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                             int mtiles, int ntiles, int splits, cudaStream_t st);
-cudaError_t tc_wgrad_reduce(const float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh,
-                            int kw, int layout, cudaStream_t st);
+// Split groups of the two-pass reduction (0: one pass).  With many splits, the
+// first pass sums each of G contiguous split ranges into planes that follow the
+// split planes in the workspace, so the workspace holds splits + G planes.
+int tc_wgrad_groups(int splits);
+// ws: [splits + tc_wgrad_groups(splits)][Nx * kn] FP32.
+cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh, int kw,
+                            int layout, cudaStream_t st);

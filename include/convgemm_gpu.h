@@ -57,6 +57,10 @@ typedef struct {
 
 /* Status and message of the last failing call on this host thread. */
 convgemm_status_t convgemm_get_last_status(void);
+
+/* Number of GPU kernels the library has launched (or recorded into a stream
+ * capture) in this process: a diagnostic for counting launches per step. */
+unsigned long long convgemm_launch_count(void);
 const char *convgemm_get_last_error(void);
 void convgemm_clear_error(void);
 /* Reads (and clears) the device-side error word that bounded waits set; it

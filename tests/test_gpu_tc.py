@@ -133,6 +133,8 @@ WGRAD_SHAPES = [
     (1, 12, 10, 40, 96, 3, 2, 1, 2),      # kn = 96, dilation
     (8, 28, 28, 128, 128, 3, 1, 1, 1),    # several pixel splits
     (2, 9, 9, 16, 256, 1, 0, 2, 1),       # Nx = 16: BN = 64 on the X side
+    (8, 56, 56, 64, 256, 1, 0, 1, 1),     # 49 splits: two-pass grouped reduction, dY is A
+    (8, 56, 56, 256, 64, 1, 0, 1, 1),     # 49 splits, X is A
 ]
 
 
