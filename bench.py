@@ -209,6 +209,10 @@ class Net:
                 ws_f32 = max(ws_f32, cg.wgrad_f32_workspace_size(s))
             self.L.append(d)
         self.ws = torch.empty(ws_bf16 // 4 + 1, device=dev)
+        # every layer's BN fold and weight packings in one grouped launch
+        self.prep = tc.Prep([dict(layout=cg.NHWC, shape=d["s"], weights=d["w32"], packed_fwd=d["wp"],
+                                  packed_dgrad=d["wpd"], mean=d["mean"], inv_std=d["inv_std"], gamma=d["gamma"],
+                                  beta=d["beta"], scale=d["scale"], shift=d["shift"]) for d in self.L])
         self.ws32 = torch.empty(ws_f32 // 4 + 1, device=dev) if with_fp32 else None
         self.with_fp32 = with_fp32
         if with_fp32:
@@ -224,6 +228,26 @@ class Net:
     def launches_f32(self):
         return sum(3 if d["first"] else 4 for d in self.L)
 
+    def tune_items(self):
+        """(operation, shape, launcher) of every BF16 convolution of the step, for the autotuner."""
+        tc, cg = self.tc, self.cg
+        items = []
+        for d in self.L:
+            s = d["s"]
+            items.append({"op": tc.TUNE_FWD, "shape": s, "run": lambda ws, d=d, s=s: tc.fwd_bf16(
+                s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"])})
+            if not d["first"]:
+                items.append({"op": tc.TUNE_DGRAD, "shape": s,
+                              "run": lambda ws, d=d, s=s: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"])})
+            items.append({"op": tc.TUNE_WGRAD, "shape": s, "run": lambda ws, d=d, s=s: tc.wgrad_bf16(
+                cg.NHWC, s, d["dy"], d["x"], d["dw"], ws)})
+        return items
+
+    def resize_workspace(self):
+        need = max(self.tc.wgrad_bf16_workspace_size(d["s"]) for d in self.L)
+        if need > self.ws.numel() * 4:
+            self.ws = self.torch.empty(need // 4 + 1, device="cuda")
+
     def step_bf16(self):
         """One BF16 step: weight preparation, forward, input gradient, weight gradient of every layer."""
         for fam in ("prep", "fwd", "dgrad", "wgrad"):
@@ -233,17 +257,12 @@ class Net:
         """Launches one kernel family of the BF16 step; returns how many kernels it launched."""
         tc, cg = self.tc, self.cg
         n = 0
+        if fam == "prep":
+            self.prep.launch()
+            return 1
         for d in self.L:
             s = d["s"]
-            if fam == "prep":
-                tc.fold_epilogue(s.kn, d["scale"], d["shift"], mean=d["mean"], inv_std=d["inv_std"],
-                                 gamma=d["gamma"], beta=d["beta"])
-                tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
-                n += 2 + (1 if (s.kh * s.kw * c8(s.c)) % 64 else 0)
-                if not d["first"]:
-                    tc.pack_weights(cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
-                    n += 1
-            elif fam == "fwd":
+            if fam == "fwd":
                 tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"])
                 n += 1
             elif fam == "dgrad" and not d["first"]:
@@ -956,6 +975,8 @@ def main():
     ap.add_argument("--workload", default="resnet50", choices=["resnet50", "grouped", "vgg16", "forms"],
                     help="resnet50: the headline fwd+bwd step; grouped: uneven convolutions in one launch")
     ap.add_argument("--group-n", type=int, default=256)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="built-in tile heuristics only (no tuning table)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -969,7 +990,7 @@ def main():
 
     import torch
     import convgemm_gb300 as cg
-    from convgemm_gb300 import tc
+    from convgemm_gb300 import autotune, tc
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -985,6 +1006,14 @@ def main():
         return run_only(torch, cg, tc, layers, batch, args)
     net = Net(torch, cg, tc, layers, batch, with_fp32=not args.no_fp32)
     flops = step_flops(layers, batch)
+
+    # per-shape tile configuration: tuning table (cached / shipped / measured now)
+    net.step_family("prep")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tune_stats = None if args.no_autotune else autotune.tune_ops(net.tune_items())
+    tune_s = time.perf_counter() - t0
+    net.resize_workspace()
 
     # warm every launch path once outside any capture (attribute setup, error word)
     net.step_bf16()
@@ -1101,7 +1130,8 @@ def main():
                            "global_batch": batch * world, "per_gpu_batch": batch, "seq_len": None,
                            "parallelism": f"replicas{world}", "step": "one CUDA graph replay",
                            "l2": "inputs larger than L2 (per-step working set of several GB)",
-                           "gflop_per_img": flops / batch / 1e9},
+                           "gflop_per_img": flops / batch / 1e9,
+                           "autotune": tune_stats, "autotune_s": tune_s},
                 "tflops": flops / (ms / 1000) / 1e12,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "fp32_plain": fp32,
                 "bf16_vs_fp32": (value / fp32["value"]) if fp32 else None,

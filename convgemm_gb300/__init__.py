@@ -116,6 +116,12 @@ def lib():
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_launch_count.restype = ctypes.c_ulonglong
+        L.convgemm_tune_set.argtypes = [_I, SP, _I, _I]
+        L.convgemm_wgrad_bf16_plan.argtypes = [SP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]
+        L.convgemm_prep_table_size.argtypes = [_I]
+        L.convgemm_prep_table_size.restype = ctypes.c_size_t
+        L.convgemm_prep_prepare.argtypes = [_I, _VP, _VP, ctypes.c_size_t, ctypes.POINTER(_I), ctypes.POINTER(_I)]
+        L.convgemm_prep_launch.argtypes = [_VP, _I, _I, _VP]
         L.convgemm_group_weights_size.argtypes = [SP]
         L.convgemm_group_weights_size.restype = ctypes.c_size_t
         L.convgemm_group_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP]

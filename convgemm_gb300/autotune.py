@@ -130,3 +130,109 @@ def tune(convs, path: str | None = None, force: bool = False):
     if dirty:
         _save(path, db)
     return out
+
+
+# ------------------------------------------------ single-convolution operations
+# The forward, input-gradient and weight-gradient entry points take their tile
+# configuration from the library's tuning table (convgemm_tune_set) when it has
+# an entry for the shape.  tune_ops measures the candidates of each (operation,
+# shape) -- tile widths, and for the weight gradient also pixel-split counts --
+# with `reps` calls replayed from one CUDA graph (device time, no host launch
+# cost), installs the fastest and caches it beside the grouped-launch widths.
+
+OP_NAMES = {tc.TUNE_FWD: "fwd", tc.TUNE_DGRAD: "dgrad", tc.TUNE_WGRAD: "wgrad", tc.TUNE_FWD_FP8: "fwd_fp8",
+            tc.TUNE_FWD_BF16X3: "fwd_bf16x3"}
+
+
+def op_key(op: int, s) -> str:
+    return f"{OP_NAMES[op]}|{shape_key(s)}"
+
+
+def graph_time_us(run, reps: int = 10) -> float:
+    import torch
+    run()
+    torch.cuda.synchronize()
+    st = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(st):
+        run()
+        st.synchronize()
+        with torch.cuda.graph(g, stream=st):
+            for _ in range(reps):
+                run()
+    torch.cuda.synchronize()
+    g.replay()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    g.replay()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) * 1000 / reps
+
+
+def op_candidates(op: int, s):
+    """(bn, splits) candidates; splits 0 = heuristic (only the weight gradient varies it)."""
+    if op == tc.TUNE_DGRAD:
+        return [(w, 0) for w in candidate_widths(s.c)]
+    if op != tc.TUNE_WGRAD:
+        return [(w, 0) for w in candidate_widths(s.kn)]
+    tc.tune_set(op, s, 0, 0)
+    bn0, s0, mx = tc.wgrad_bf16_plan(s)
+    widths = [64, 128] if s.kn < 128 else candidate_widths(s.kh * s.kw * tc.c8(s.c))
+    splits = sorted({max(1, s0 // 4), max(1, s0 // 2), s0, min(mx, 2 * s0)})
+    return [(w, sp) for w in widths for sp in splits]
+
+
+def tune_ops(items, path: str | None = None, force: bool = False, measure_missing: bool = True,
+             ws_limit_bytes: int = 1 << 30):
+    """items: dicts {"op": tc.TUNE_*, "shape": Shape, "run": callable(workspace)}; run(ws) launches
+    the operation once (the workspace argument matters to the weight gradient only).
+
+    Installs the chosen configuration of every item in the library and returns
+    {"measured": n, "cached": n, "shipped": n}.
+    """
+    import torch
+    path = path or cache_path()
+    dev = torch.cuda.get_device_properties(torch.cuda.current_device())
+    db = _load(path)
+    table = db.setdefault(dev.name, {})
+    shipped = {} if force else _load(SHIPPED).get(dev.name, {})
+    stats = {"measured": 0, "cached": 0, "shipped": 0, "heuristic": 0}
+    dirty = False
+    for it in items:
+        op, s = it["op"], it["shape"]
+        k = op_key(op, s)
+        entry = None
+        if not force and k in table:
+            entry, src = table[k], "cached"
+        elif not force and k in shipped:
+            entry, src = shipped[k], "shipped"
+        elif measure_missing:
+            best, times = None, {}
+            for bn, sp in op_candidates(op, s):
+                tc.tune_set(op, s, bn, sp)
+                ws = None
+                if op == tc.TUNE_WGRAD:
+                    nbytes = tc.wgrad_bf16_workspace_size(s)
+                    if nbytes > ws_limit_bytes:
+                        continue
+                    ws = torch.empty(nbytes // 4 + 1, device="cuda")
+                us = graph_time_us(lambda: it["run"](ws))
+                times[f"{bn}/{sp}"] = us
+                if best is None or us < best[0]:
+                    best = (us, bn, sp)
+            tc.tune_set(op, s, 0, 0)
+            if best is None:
+                stats["heuristic"] += 1
+                continue
+            entry, src = {"bn": best[1], "splits": best[2], "us": times}, "measured"
+            table[k] = entry
+            dirty = True
+        else:
+            stats["heuristic"] += 1
+            continue
+        tc.tune_set(op, s, int(entry["bn"]), int(entry.get("splits", 0)))
+        stats[src] += 1
+    if dirty:
+        _save(path, db)
+    return stats

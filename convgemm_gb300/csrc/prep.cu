@@ -203,6 +203,98 @@ __global__ void pack_split_kernel(const float *__restrict__ w, int nchw, int C, 
     }
 }
 
+// Grouped preparation: every block finds its job by binary search over the jobs'
+// first blocks and runs that job's body for its block (256 threads).
+// The jobs' first blocks (b0, njobs ints) are staged in shared memory first, so the
+// search costs one global round trip.
+__global__ void __launch_bounds__(256) prep_group_kernel(const PrepJob *__restrict__ jobs, const int *__restrict__ b0,
+                                                         int njobs) {
+    __shared__ float tile[32][33];
+    extern __shared__ int s_b0[];
+    for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_b0[i] = __ldg(b0 + i);
+    __syncthreads();
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_b0[mid] <= (int) blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const PrepJob &J = jobs[lo];
+    const int lb = blockIdx.x - J.block0;
+    const int t = threadIdx.x;
+    switch (J.type) {
+        case PREP_FOLD: {
+            const int n = lb * 256 + t;
+            if (n >= J.kn) return;
+            double sc = 1.0, sh = J.bias ? (double) J.bias[n] : 0.0;
+            if (J.mean) {
+                sc = (double) J.gamma[n] * (double) J.inv_std[n];
+                sh = (double) J.beta[n] + (sh - (double) J.mean[n]) * sc;
+            }
+            J.scale[n] = (float) sc;
+            J.shift[n] = (float) sh;
+            return;
+        }
+        case PREP_FWD_TILED: {
+            // the tiled transpose of pack_fwd_tiled_kernel for one (ci tile, co tile), all taps
+            const int nci = (J.Cp + 31) / 32;
+            const int ci0 = (lb % nci) * 32, co0 = (lb / nci) * 32;
+            const int tx = t & 31, ty = t >> 5, khw = J.kh * J.kw;
+            bf16 *out = (bf16 *) J.out;
+            for (int tap = 0; tap < khw; tap++) {
+                for (int i = ty; i < 32; i += 8) {
+                    const int ci = ci0 + i, co = co0 + tx;
+                    tile[i][tx] = (ci < J.C && co < J.kn) ? J.w[((size_t) ci * khw + tap) * J.kn + co] : 0.0f;
+                }
+                __syncthreads();
+                for (int j = ty; j < 32; j += 8) {
+                    const int co = co0 + j, ci = ci0 + tx;
+                    if (co < J.kn && ci < J.Cp)
+                        out[(size_t) co * J.Kpad + (size_t) tap * J.Cp + ci] = __float2bfloat16_rn(tile[tx][j]);
+                }
+                __syncthreads();
+            }
+            return;
+        }
+        case PREP_FWD_ELEM: {
+            // block = (row co, 256 columns of K): 32-bit index math, no division by the row length
+            const int nch = (J.Kpad + 255) / 256;
+            const int co = lb / nch, k = (lb % nch) * 256 + t;
+            if (k >= J.Kpad) return;
+            const int tap = k / J.Cp, ci = k - tap * J.Cp;
+            float v = 0.0f;
+            if (tap < J.kh * J.kw && ci < J.C) v = wref(J.w, J.nchw, J.C, J.kh, J.kw, J.kn, ci, tap / J.kw, tap % J.kw, co);
+            ((bf16 *) J.out)[(size_t) co * J.Kpad + k] = __float2bfloat16_rn(v);
+            return;
+        }
+        case PREP_FWD_TAIL: {
+            const int kbeg = J.kh * J.kw * J.Cp, width = J.Kpad - kbeg;
+            const int i = lb * 256 + t;
+            if (i >= J.kn * width) return;
+            const int co = i / width;
+            ((bf16 *) J.out)[(size_t) co * J.Kpad + kbeg + (i - co * width)] = __float2bfloat16_rn(0.0f);
+            return;
+        }
+        default: {   // PREP_DGRAD: block = (4 input channels, one stride-phase class): the class's
+                     // K segment of those rows, taps x knp output channels and the K padding after them
+            const int c = lb % J.info.ncls, ci0 = (lb / J.info.ncls) * 4;
+            const int beg = J.info.kbeg[c], end = c + 1 < J.info.ncls ? J.info.kbeg[c + 1] : J.info.Ktot;
+            const int nt = J.info.ntaps[c];
+            for (int r = 0; r < 4; r++) {
+                const int ci = ci0 + r;
+                if (ci >= J.C) break;
+                bf16 *row = (bf16 *) J.out + (size_t) ci * J.info.Ktot + beg;
+                for (int idx = t; idx < end - beg; idx += 256) {
+                    const int g = (int) J.dknp.div((uint32_t) idx), co = idx - g * J.knp;
+                    float v = 0.0f;
+                    if (g < nt && co < J.kn) v = wref(J.w, J.nchw, J.C, J.kh, J.kw, J.kn, ci, J.info.kx[c][g], J.info.ky[c][g], co);
+                    row[idx] = __float2bfloat16_rn(v);
+                }
+            }
+        }
+    }
+}
+
 int grid_for(long long n) {
     long long g = (n + 255) / 256;
     return (int) (g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
@@ -277,5 +369,11 @@ cudaError_t prep_pack_split(const float *w, int nchw, int C, int kh, int kw, int
                             void *lo, cudaStream_t st) {
     pack_split_kernel<<<grid_for((long long) kn * Kpad), 256, 0, st>>>(w, nchw, C, kh, kw, kn, Cp, Kpad, (bf16 *) hi,
                                                                       (bf16 *) lo); cg_note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t prep_group_launch(const PrepJob *jobs, int njobs, int nblocks, cudaStream_t st) {
+    const int *b0 = (const int *) (jobs + njobs);
+    prep_group_kernel<<<nblocks, 256, sizeof(int) * njobs, st>>>(jobs, b0, njobs); cg_note_launch();
     return cudaGetLastError();
 }

@@ -11,6 +11,23 @@ struct PackDgradInfo {
     int8_t kx[TC_MAXCLS][TC_MAXTAPS], ky[TC_MAXCLS][TC_MAXTAPS];
 };
 
+// One job of the grouped preparation launch (prep_group_launch): a block range of
+// one batch-norm fold or one weight packing.
+enum { PREP_FOLD = 0, PREP_FWD_TILED = 1, PREP_FWD_ELEM = 2, PREP_FWD_TAIL = 3, PREP_DGRAD = 4 };
+struct PrepJob {
+    int type, block0, nblocks;                 // blocks [block0, block0 + nblocks) of the launch
+    int nchw, C, kh, kw, kn, Cp, Kpad, knp;    // weight geometry (packing jobs)
+    const float *w;
+    void *out;
+    const float *bias, *mean, *inv_std, *gamma, *beta;   // fold job
+    float *scale, *shift;
+    PackDgradInfo info;                        // input-gradient packing job
+    FastDiv dknp;                              // division by knp
+};
+// jobs: device array sorted by block0, followed by the njobs block0 values as ints
+// (at most 12288 jobs); nblocks: total blocks of all jobs.
+cudaError_t prep_group_launch(const PrepJob *jobs, int njobs, int nblocks, cudaStream_t st);
+
 cudaError_t prep_pack_fwd(const float *w, int nchw, int C, int kh, int kw, int kn, int Cp, int Kpad, void *out,
                           cudaStream_t st);
 cudaError_t prep_pack_dgrad(const float *w, int nchw, int C, int kh, int kw, int kn, int knp,

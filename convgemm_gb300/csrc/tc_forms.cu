@@ -81,7 +81,9 @@ extern "C" convgemm_status_t convgemm_fwd_fp8(const convgemm_shape_t *shape, con
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     tc_plan_fwd(s, pl);
-    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 1);
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_FWD_FP8, *shape, &t);
+    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 1, nullptr, nullptr, t.bn);
 }
 
 extern "C" convgemm_status_t convgemm_split_bf16x2(size_t n, const float *in, void *hi, void *lo, void *stream) {
@@ -111,5 +113,7 @@ extern "C" convgemm_status_t convgemm_fwd_bf16x3(const convgemm_shape_t *shape, 
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     tc_plan_fwd(s, pl);
-    return tc_run(pl, s, x_hi, w_hi, y, scale, shift, relu, (cudaStream_t) stream, 2, x_lo, w_lo);
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_FWD_BF16X3, *shape, &t);
+    return tc_run(pl, s, x_hi, w_hi, y, scale, shift, relu, (cudaStream_t) stream, 2, x_lo, w_lo, t.bn);
 }

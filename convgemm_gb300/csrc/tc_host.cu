@@ -3,6 +3,7 @@
 // tensor maps, and the public convgemm_*_bf16 entry points.
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/convgemm_gpu.h"
 #include "cg_common.cuh"
@@ -276,13 +277,13 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
-                         const void *in_lo, const void *w_lo) {
+                         const void *in_lo, const void *w_lo, int bn_override) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
     TcConvParams p;
     memset(&p, 0, sizeof(p));
     p.mode = mode;
-    p.bn = tc_pick_bn(pl, sms);
+    p.bn = bn_override ? bn_override : tc_pick_bn(pl, sms);
     const int eb = mode == 1 ? 1 : 2;   // operand element bytes
     CUtensorMap wmap, omap;
     if (convgemm_status_t e = tc_make_map_2d_sw(&wmap, eb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
@@ -442,7 +443,9 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     tc_plan_fwd(s, pl);
-    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream);
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_FWD, *shape, &t);
+    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 0, nullptr, nullptr, t.bn);
 }
 
 extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
@@ -461,7 +464,9 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, 
                 cudaMemsetAsync(dx, 0, sizeof(__nv_bfloat16) * (size_t) s.b * s.h * s.w * s.c, st), "zero dx"))
             return e;
     }
-    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st);
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
+    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn);
 }
 
 // ------------------------------------------------------- weight gradient
@@ -474,8 +479,11 @@ struct WgPlan {
     size_t ws_bytes;
 };
 
-WgPlan plan_wgrad(const cg_shape &s) {
+WgPlan plan_wgrad(const convgemm_shape_t &ps) {
+    const cg_shape s = cg_from_public(ps);
     const ConvGeom g = make_geom(s);
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_WGRAD, ps, &t);
     WgPlan w;
     w.Cp = round_up(s.c, 8);
     w.kn8 = round_up(s.kn, 8);
@@ -486,10 +494,12 @@ WgPlan plan_wgrad(const cg_shape &s) {
         Mext = w.Nx;
         Next = s.kn;
         w.bn = s.kn <= 64 ? 64 : 128;
+        if (t.bn == 64 || t.bn == 128) w.bn = t.bn;
     } else {
         Mext = s.kn;
         Next = w.Nx;
         w.bn = w.Nx >= 256 ? 256 : (w.Nx > 64 ? 128 : 64);
+        if (t.bn) w.bn = t.bn;
     }
     w.mtiles = (Mext + 127) / 128;
     w.ntiles = (Next + w.bn - 1) / w.bn;
@@ -499,6 +509,7 @@ WgPlan plan_wgrad(const cg_shape &s) {
     int splits = tc_num_sms() * per_sm / base;   // one wave: no partial second wave
     const int max_splits = (w.nchunks + 7) / 8;  // at least 8 chunks (512 pixels) per split
     if (splits > max_splits) splits = max_splits;
+    if (t.splits) splits = t.splits < w.nchunks ? t.splits : w.nchunks;
     if (splits < 1) splits = 1;
     w.cps = (w.nchunks + splits - 1) / splits;
     w.splits = (w.nchunks + w.cps - 1) / w.cps;
@@ -508,9 +519,19 @@ WgPlan plan_wgrad(const cg_shape &s) {
 
 }  // namespace
 
+extern "C" convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *shape, int *bn, int *splits,
+                                                      int *max_splits) {
+    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_wgrad_bf16_plan")) return e;
+    const WgPlan w = plan_wgrad(*shape);
+    if (bn) *bn = w.bn;
+    if (splits) *splits = w.splits;
+    if (max_splits) *max_splits = w.nchunks;
+    return CONVGEMM_SUCCESS;
+}
+
 extern "C" size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape) {
     if (check_tc_shape(shape, "convgemm_wgrad_bf16_workspace_size")) return 0;
-    return plan_wgrad(cg_from_public(*shape)).ws_bytes;
+    return plan_wgrad(*shape).ws_bytes;
 }
 
 extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_shape_t *shape,
@@ -523,7 +544,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_wgrad_bf16: bad layout %d", (int) layout);
     const cg_shape s = cg_from_public(*shape);
     const ConvGeom g = make_geom(s);
-    const WgPlan w = plan_wgrad(s);
+    const WgPlan w = plan_wgrad(*shape);
     if (workspace_bytes < w.ws_bytes)
         return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "convgemm_wgrad_bf16: workspace %zu bytes < %zu needed",
                             workspace_bytes, w.ws_bytes);
@@ -574,4 +595,120 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     return cg_cuda_check(tc_wgrad_reduce((float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
                                          s.kw, layout == CONVGEMM_NCHW, st),
                          "weight-gradient reduction");
+}
+
+// ------------------------------------------------- grouped weight preparation
+// The batch-norm folds and weight packings of many layers in one launch (a
+// training step re-packs every layer's FP32 master weights): the host builds a
+// job table once, the launch is capturable in a CUDA graph.
+
+extern "C" size_t convgemm_prep_table_size(int n) {
+    return n > 0 ? (size_t) 4 * n * (sizeof(PrepJob) + sizeof(int)) : 0;
+}
+
+extern "C" convgemm_status_t convgemm_prep_prepare(int n, const convgemm_prep_item_t *items, void *table,
+                                                   size_t table_bytes, int *njobs, int *nblocks) {
+    const char *fn = "convgemm_prep_prepare";
+    if (n < 1 || !items || !table || !njobs || !nblocks)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: bad arguments", fn);
+    if (table_bytes < convgemm_prep_table_size(n) || ((uintptr_t) table & 15))
+        return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "%s: table needs %zu bytes, 16-byte aligned", fn,
+                            convgemm_prep_table_size(n));
+    std::vector<PrepJob> jobs;
+    long long blocks = 0;
+    auto add = [&](PrepJob j, long long nb) {
+        if (nb <= 0) return;
+        j.block0 = (int) blocks;
+        j.nblocks = (int) nb;
+        jobs.push_back(j);
+        blocks += nb;
+    };
+    for (int i = 0; i < n; i++) {
+        const convgemm_prep_item_t &it = items[i];
+        if (convgemm_status_t e = check_tc_shape(&it.shape, fn)) return e;
+        if (it.layout != CONVGEMM_NHWC && it.layout != CONVGEMM_NCHW)
+            return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: item %d: bad layout", fn, i);
+        if ((it.packed_fwd || it.packed_dgrad) && !it.weights)
+            return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: item %d: packing without weights", fn, i);
+        if (!it.scale != !it.shift)
+            return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: item %d: scale and shift go together", fn, i);
+        if (it.epi.mean && !(it.epi.inv_std && it.epi.gamma && it.epi.beta))
+            return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: item %d: batch-norm needs all parameters", fn, i);
+        const cg_shape s = cg_from_public(it.shape);
+        PrepJob j;
+        memset(&j, 0, sizeof(j));
+        j.nchw = it.layout == CONVGEMM_NCHW;
+        j.C = s.c;
+        j.kh = s.kh;
+        j.kw = s.kw;
+        j.kn = s.kn;
+        j.w = it.weights;
+        if (it.scale) {
+            PrepJob f = j;
+            f.type = PREP_FOLD;
+            f.bias = it.epi.bias;
+            f.mean = it.epi.mean;
+            f.inv_std = it.epi.inv_std;
+            f.gamma = it.epi.gamma;
+            f.beta = it.epi.beta;
+            f.scale = it.scale;
+            f.shift = it.shift;
+            add(f, (s.kn + 255) / 256);
+        }
+        if (it.packed_fwd) {
+            TcPlan pl;
+            tc_plan_fwd(s, pl);
+            PrepJob f = j;
+            f.Cp = pl.Cin;
+            f.Kpad = pl.Ktot;
+            f.out = it.packed_fwd;
+            const int khw = s.kh * s.kw;
+            if (j.nchw) {
+                f.type = PREP_FWD_ELEM;
+                add(f, (long long) s.kn * ((f.Kpad + 255) / 256));
+            } else {
+                f.type = PREP_FWD_TILED;
+                add(f, (long long) ((f.Cp + 31) / 32) * ((s.kn + 31) / 32));
+                if (f.Kpad > khw * f.Cp) {
+                    if ((long long) s.kn * (f.Kpad - khw * f.Cp) > (1LL << 31) - 256)
+                        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: item %d: weights too large", fn, i);
+                    f.type = PREP_FWD_TAIL;
+                    add(f, ((long long) s.kn * (f.Kpad - khw * f.Cp) + 255) / 256);
+                }
+            }
+        }
+        if (it.packed_dgrad) {
+            TcPlan pl;
+            if (!tc_plan_dgrad(s, pl))
+                return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: item %d: more than 16 stride-phase classes", fn, i);
+            if (pl.Ktot > 0) {
+                PrepJob f = j;
+                f.type = PREP_DGRAD;
+                f.knp = pl.Cin;
+                f.info = tc_pack_info(pl);
+                f.dknp = FastDiv((uint32_t) f.knp);
+                f.out = it.packed_dgrad;
+                add(f, (long long) ((s.c + 3) / 4) * f.info.ncls);
+            }
+        }
+        if (blocks > (1LL << 31) - 1) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: too many blocks", fn);
+    }
+    if (jobs.empty()) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: nothing to prepare", fn);
+    if (jobs.size() > 12288) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: more than 12288 jobs", fn);
+    *njobs = (int) jobs.size();
+    *nblocks = (int) blocks;
+    // [jobs][block0 of each job]
+    std::vector<uint8_t> bytes(sizeof(PrepJob) * jobs.size() + sizeof(int) * jobs.size());
+    memcpy(bytes.data(), jobs.data(), sizeof(PrepJob) * jobs.size());
+    for (size_t j = 0; j < jobs.size(); j++)
+        memcpy(bytes.data() + sizeof(PrepJob) * jobs.size() + sizeof(int) * j, &jobs[j].block0, sizeof(int));
+    return cg_cuda_check(cudaMemcpy(table, bytes.data(), bytes.size(), cudaMemcpyHostToDevice),
+                         "copy preparation table");
+}
+
+extern "C" convgemm_status_t convgemm_prep_launch(const void *table, int njobs, int nblocks, void *stream) {
+    if (!table || njobs < 1 || nblocks < 1)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_prep_launch: bad arguments");
+    return cg_cuda_check(prep_group_launch((const PrepJob *) table, njobs, nblocks, (cudaStream_t) stream),
+                         "grouped preparation launch");
 }

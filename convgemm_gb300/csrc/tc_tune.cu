@@ -1,0 +1,50 @@
+// Per-shape tile configuration chosen by the autotuner (convgemm_gb300/autotune.py):
+// the output-channel width of a tile (64 / 128 / 256) for the forward and
+// input-gradient kernels, and the tile width and pixel-split count of the
+// weight gradient.  Shapes without an entry use the built-in heuristics.
+#include <array>
+#include <map>
+#include <mutex>
+
+#include "../../include/convgemm_gpu.h"
+#include "tc_host.h"
+
+namespace {
+
+using Key = std::array<int, 14>;
+std::mutex g_tune_mu;
+std::map<Key, TcTune> g_tune;
+
+Key key_of(int op, const convgemm_shape_t &s) {
+    return {op, s.b, s.h, s.w, s.c, s.kn, s.kh, s.kw, s.vpad, s.hpad, s.vstride, s.hstride, s.vdil, s.hdil};
+}
+
+}  // namespace
+
+bool tc_tune_get(int op, const convgemm_shape_t &s, TcTune *t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key_of(op, s));
+    if (it == g_tune.end()) return false;
+    *t = it->second;
+    return true;
+}
+
+extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int splits) {
+    if (!shape || op < CONVGEMM_TUNE_FWD || op > CONVGEMM_TUNE_FWD_BF16X3)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: bad operation or NULL shape");
+    if (bn != 0 && bn != 64 && bn != 128 && bn != 256)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: tile width %d is not 0/64/128/256", bn);
+    if (splits < 0 || (splits > 0 && op != CONVGEMM_TUNE_WGRAD))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: splits apply to the weight gradient only");
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (bn == 0 && splits == 0)
+        g_tune.erase(key_of(op, *shape));
+    else
+        g_tune[key_of(op, *shape)] = TcTune{bn, splits};
+    return CONVGEMM_SUCCESS;
+}
+
+extern "C" void convgemm_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}

@@ -48,6 +48,26 @@ def wgrad_bf16_workspace_size(shape: Shape) -> int:
     return lib().convgemm_wgrad_bf16_workspace_size(ctypes.byref(shape))
 
 
+def wgrad_bf16_plan(shape: Shape):
+    """(tile width, pixel splits, largest useful split count) of the weight gradient."""
+    bn, sp, mx = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _raise_if(lib().convgemm_wgrad_bf16_plan(ctypes.byref(shape), ctypes.byref(bn), ctypes.byref(sp),
+                                             ctypes.byref(mx)))
+    return bn.value, sp.value, mx.value
+
+
+TUNE_FWD, TUNE_DGRAD, TUNE_WGRAD, TUNE_FWD_FP8, TUNE_FWD_BF16X3 = range(5)
+
+
+def tune_set(op: int, shape: Shape, bn: int = 0, splits: int = 0):
+    """Overrides the tile heuristics for one operation on one shape (0, 0 removes the entry)."""
+    _raise_if(lib().convgemm_tune_set(op, ctypes.byref(shape), bn, splits))
+
+
+def tune_clear():
+    lib().convgemm_tune_clear()
+
+
 def wgrad_bf16(layout, shape: Shape, dy, x, dw, workspace, stream=None):
     nbytes = workspace.numel() * workspace.element_size()
     _raise_if(lib().convgemm_wgrad_bf16(layout, ctypes.byref(shape), ptr(dy), ptr(x), ptr(dw), ptr(workspace),
@@ -139,3 +159,41 @@ class Group:
 
     def launch(self, stream=None):
         _raise_if(lib().convgemm_group_launch(self._tptr, self.n, self.tiles, _stream(stream)))
+
+
+# ------------------------------------------------------ grouped weight preparation
+class PrepItem(ctypes.Structure):
+    """convgemm_prep_item_t (include/convgemm_gpu.h)."""
+    _fields_ = [("layout", ctypes.c_int), ("shape", Shape), ("weights", ctypes.c_void_p),
+                ("packed_fwd", ctypes.c_void_p), ("packed_dgrad", ctypes.c_void_p), ("epi", Epilogue),
+                ("scale", ctypes.c_void_p), ("shift", ctypes.c_void_p)]
+
+
+class Prep:
+    """Batch-norm folds and weight packings of many layers in one launch.
+
+    items: dicts with layout, shape, weights and any of packed_fwd, packed_dgrad,
+    scale + shift (with bias / mean / inv_std / gamma / beta).  The job table is
+    built once here; launch() may be captured in a CUDA graph.
+    """
+
+    def __init__(self, items, device="cuda"):
+        import torch
+        n = len(items)
+        arr = (PrepItem * n)()
+        for i, it in enumerate(items):
+            e = Epilogue(ptr(it.get("bias")), ptr(it.get("mean")), ptr(it.get("inv_std")), ptr(it.get("gamma")),
+                         ptr(it.get("beta")), 0)
+            arr[i] = PrepItem(int(it["layout"]), it["shape"], ptr(it.get("weights")), ptr(it.get("packed_fwd")),
+                              ptr(it.get("packed_dgrad")), e, ptr(it.get("scale")), ptr(it.get("shift")))
+        nbytes = lib().convgemm_prep_table_size(n)
+        self.table = torch.empty(nbytes + 16, dtype=torch.uint8, device=device)
+        self._tptr = self.table.data_ptr() + (-self.table.data_ptr()) % 16
+        nj, nb = ctypes.c_int(0), ctypes.c_int(0)
+        _raise_if(lib().convgemm_prep_prepare(n, ctypes.cast(arr, ctypes.c_void_p), self._tptr, nbytes,
+                                              ctypes.byref(nj), ctypes.byref(nb)))
+        self.njobs, self.nblocks = nj.value, nb.value
+        self._keep = items
+
+    def launch(self, stream=None):
+        _raise_if(lib().convgemm_prep_launch(self._tptr, self.njobs, self.nblocks, _stream(stream)))

@@ -166,6 +166,53 @@ convgemm_status_t convgemm_fwd_bf16x3(const convgemm_shape_t *shape, const void 
                                       const void *w_hi, const void *w_lo, float *y, const float *scale,
                                       const float *shift, int relu, void *stream);
 
+/* ------------------------------------------------ grouped weight preparation */
+
+/* One layer's preparation for the BF16 forms: pack its FP32 weights (reference
+ * layout of `layout`) into the forward and/or input-gradient operands, and fold
+ * its bias / batch-norm into scale / shift (FP64 arithmetic).  NULL outputs are
+ * skipped. */
+typedef struct {
+    convgemm_layout_t layout;
+    convgemm_shape_t shape;
+    const float *weights;
+    void *packed_fwd;        /* convgemm_bf16_weights_size(shape, CONVGEMM_OPERAND_FWD) bytes, or NULL */
+    void *packed_dgrad;      /* convgemm_bf16_weights_size(shape, CONVGEMM_OPERAND_DGRAD) bytes, or NULL */
+    convgemm_epilogue_t epi; /* fold parameters (relu is not used here) */
+    float *scale;            /* kn floats, or NULL (no fold) */
+    float *shift;
+} convgemm_prep_item_t;
+
+/* Bytes of the device job table for n items (16-byte aligned memory). */
+size_t convgemm_prep_table_size(int n);
+/* Builds the job table of n items (synchronous copy: outside stream capture);
+ * returns the job and block counts for the launch. */
+convgemm_status_t convgemm_prep_prepare(int n, const convgemm_prep_item_t *items, void *table, size_t table_bytes,
+                                        int *njobs, int *nblocks);
+/* Every fold and packing of the table in one launch (capturable in a CUDA graph);
+ * results are identical to the per-layer calls. */
+convgemm_status_t convgemm_prep_launch(const void *table, int njobs, int nblocks, void *stream);
+
+/* ------------------------------------------------ autotuned tile configuration */
+
+/* Operations a tile configuration can be set for. */
+enum {
+    CONVGEMM_TUNE_FWD = 0,        /* convgemm_fwd_bf16 */
+    CONVGEMM_TUNE_DGRAD = 1,      /* convgemm_dgrad_bf16 */
+    CONVGEMM_TUNE_WGRAD = 2,      /* convgemm_wgrad_bf16 (and its workspace size) */
+    CONVGEMM_TUNE_FWD_FP8 = 3,    /* convgemm_fwd_fp8 */
+    CONVGEMM_TUNE_FWD_BF16X3 = 4  /* convgemm_fwd_bf16x3 */
+};
+
+/* Process-wide override of the built-in heuristics for one operation on one
+ * shape, as chosen by an autotuner: bn = output channels per tile (64, 128 or
+ * 256; for the weight gradient the width of its N side), splits = pixel splits
+ * of the weight gradient (0 = heuristic; weight gradient only).  bn = splits =
+ * 0 removes the entry.  Set the weight-gradient entry before querying its
+ * workspace size.  Thread-safe. */
+convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int splits);
+void convgemm_tune_clear(void);
+
 /* ----------------------------------------- grouped persistent forward launch */
 
 /* One convolution of a grouped launch: BF16 NHWC x [b][h][w][c] (c % 8 == 0),
@@ -198,6 +245,11 @@ convgemm_status_t convgemm_group_prepare(int n, const convgemm_group_conv_t *con
 
 /* All n convolutions in one persistent launch (capturable in a CUDA graph). */
 convgemm_status_t convgemm_group_launch(const void *table, int n, int total_tiles, void *stream);
+
+/* The weight gradient's current plan for a shape (after any convgemm_tune_set
+ * entry): tile width of its N side, pixel splits, and the largest useful split
+ * count (the number of 64-pixel chunks).  Any pointer may be NULL. */
+convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *shape, int *bn, int *splits, int *max_splits);
 
 /* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
 size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);

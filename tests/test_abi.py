@@ -95,3 +95,14 @@ def test_group_prepare_rejects_bad_arguments_without_gpu(cglib):
     st = L.convgemm_group_prepare(1, ctypes.addressof(conv), addr, L.convgemm_group_table_size(1), ctypes.byref(tiles))
     assert st != 0 and "c % 8" in cglib.last_error()[1]
     assert L.convgemm_group_table_size(4) == 4 * L.convgemm_group_table_size(1) > 0
+
+
+def test_tune_table_validation_without_gpu(cglib):
+    from convgemm_gb300 import tc
+    s = cglib.Shape.of(2, 8, 8, 64, 64, 3, 3, 1, 1)
+    L = cglib.lib()
+    assert L.convgemm_tune_set(9, ctypes.byref(s), 64, 0) == 1
+    assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 96, 0) == 1
+    assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 64, 4) == 1      # splits: weight gradient only
+    assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 0, 3) == 0
+    tc.tune_clear()

@@ -182,3 +182,89 @@ def test_wgrad_bf16_rejects_small_workspace(cglib):
     with pytest.raises(cg.ConvGemmError) as ei:
         tc.wgrad_bf16(cg.NHWC, s, dy, x, dw, ws)
     assert ei.value.status == 6
+
+
+def test_tuned_tile_configurations_agree(cglib, oracle_lib):
+    """Every tile width of the tuning table gives the same forward / input-gradient result
+    (the K order of an output does not depend on the tile width); every weight-gradient
+    split count stays within tolerance of FP64 and is reproducible."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn = 4, 14, 14, 128, 192
+    s = cg.Shape.of(b, h, w, c, kn, 3, 3, 1, 1, 1, 1)
+    g = C.geom(b, h, w, c, kn, 3, 3, pad=1)
+    rng = np.random.default_rng(77)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    wt = (rng.standard_normal(9 * c * kn) * np.sqrt(2.0 / (9 * c))).astype(np.float32)
+    dy = rng.standard_normal(b * h * w * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, h, w)
+    wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
+    wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    try:
+        ys, dxs = [], []
+        for bn in (64, 128, 256):
+            tc.tune_set(tc.TUNE_FWD, s, bn)
+            tc.tune_set(tc.TUNE_DGRAD, s, bn)
+            y = torch.empty(b, h, w, kn, dtype=torch.bfloat16, device="cuda")
+            tc.fwd_bf16(s, xd, wp, y)
+            dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
+            tc.dgrad_bf16(s, dyd, wpd, dx)
+            ys.append(y)
+            dxs.append(dx)
+        torch.cuda.synchronize()
+        cg.check_device()
+        assert all(torch.equal(ys[0], y) for y in ys[1:])
+        assert all(torch.equal(dxs[0], d) for d in dxs[1:])
+        ref = O.wgrad_f64(C.NHWC, g, dy, x)
+        for bn, splits in ((64, 1), (256, 3), (128, 7)):
+            tc.tune_set(tc.TUNE_WGRAD, s, bn, splits)
+            assert tc.wgrad_bf16_plan(s)[:2] == (bn, splits)
+            ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+            d1, d2 = torch.empty(9 * c * kn, device="cuda"), torch.empty(9 * c * kn, device="cuda")
+            tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d1, ws)
+            tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d2, ws)
+            torch.cuda.synchronize()
+            cg.check_device()
+            assert torch.equal(d1, d2)
+            assert rel_max_rms(d1.cpu().numpy(), ref)[0] <= BF16_TOL
+    finally:
+        tc.tune_clear()
+
+
+def test_grouped_preparation_matches_per_layer_calls(cglib):
+    """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    rng = np.random.default_rng(5)
+    shapes = [(cg.NHWC, cg.Shape.of(2, 20, 20, 3, 64, 7, 7, 3, 3, 2, 2)),       # stem: K tail
+              (cg.NHWC, cg.Shape.of(2, 14, 14, 128, 256, 3, 3, 1, 1, 2, 2)),    # stride-2 dgrad classes
+              (cg.NCHW, cg.Shape.of(2, 9, 9, 40, 72, 3, 3, 1, 1, 1, 1)),        # NCHW, ragged
+              (cg.NHWC, cg.Shape.of(2, 8, 8, 256, 64, 1, 1))]
+    items, ref = [], []
+    for li, (layout, s) in enumerate(shapes):
+        K = s.c * s.kh * s.kw
+        wt = torch.from_numpy(rng.standard_normal(K * s.kn).astype(np.float32)).cuda()
+        bn = li % 2 == 0
+        ep = {k: torch.from_numpy(rng.uniform(.5, 1.5, s.kn).astype(np.float32)).cuda()
+              for k in ("bias", "mean", "inv_std", "gamma", "beta")} if bn else {
+            "bias": torch.from_numpy(rng.uniform(-.1, .1, s.kn).astype(np.float32)).cuda()}
+        it = dict(layout=layout, shape=s, weights=wt, **ep)
+        want = {}
+        for kind, key in ((tc.OPERAND_FWD, "packed_fwd"), (tc.OPERAND_DGRAD, "packed_dgrad")):
+            it[key] = torch.full((tc.weights_size(s, kind) // 2,), float("nan"), dtype=torch.bfloat16, device="cuda")
+            want[key] = torch.empty_like(it[key])
+            tc.pack_weights(layout, s, kind, wt, want[key])
+        it["scale"], it["shift"] = torch.empty(s.kn, device="cuda"), torch.empty(s.kn, device="cuda")
+        want["scale"], want["shift"] = torch.empty(s.kn, device="cuda"), torch.empty(s.kn, device="cuda")
+        tc.fold_epilogue(s.kn, want["scale"], want["shift"], **ep)
+        items.append(it)
+        ref.append(want)
+    p = tc.Prep(items)
+    p.launch()
+    torch.cuda.synchronize()
+    cg.check_device()
+    for it, want in zip(items, ref):
+        for k, v in want.items():
+            assert torch.equal(it[k].view(torch.int16) if v.dtype == torch.bfloat16 else it[k],
+                               v.view(torch.int16) if v.dtype == torch.bfloat16 else v), k
