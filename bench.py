@@ -354,6 +354,10 @@ def run_only(torch, cg, tc, layers, batch, args):
                      beta=d["beta"])
     tc.pack_weights(cg.NHWC, s, tc.OPERAND_FWD, d["w32"], d["wp"])
     tc.pack_weights(cg.NHWC, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
+    if not args.no_autotune:
+        from convgemm_gb300 import autotune
+        autotune.tune_ops(net.tune_items(), measure_missing=False)   # the step's tile configuration
+        net.resize_workspace()
     fn = {"fwd": lambda: tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"]),
           "dgrad": lambda: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"]),
           "wgrad": lambda: tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], net.ws)}[op]
