@@ -56,6 +56,20 @@ def max_over_ranks(torch, values, device="cuda"):
     return [float(v) for v in t.tolist()]
 
 
+def profile_traffic(prefixes, path=os.path.join(ROOT, "profiles", "launches_resnet50_bf16_b64.md")):
+    """DRAM bytes (read + write) per step of the kernels whose names start with one of
+    `prefixes`, from the committed ncu launch-list summary of one step (cold-cache capture)."""
+    try:
+        tot = 0.0
+        for line in open(path):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) == 5 and cells[0].startswith("`") and cells[0].strip("`").startswith(tuple(prefixes)):
+                tot += float(cells[4]) * 1e6
+        return tot or None
+    except (OSError, ValueError):
+        return None
+
+
 def read_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -209,6 +223,8 @@ class Net:
                 ws_f32 = max(ws_f32, cg.wgrad_f32_workspace_size(s))
             self.L.append(d)
         self.ws = torch.empty(ws_bf16 // 4 + 1, device=dev)
+        self.ws2 = self.ws
+        self.side = torch.cuda.Stream()
         # every layer's BN fold and weight packings in one grouped launch
         self.prep = tc.Prep([dict(layout=cg.NHWC, shape=d["s"], weights=d["w32"], packed_fwd=d["wp"],
                                   packed_dgrad=d["wpd"], mean=d["mean"], inv_std=d["inv_std"], gamma=d["gamma"],
@@ -247,11 +263,43 @@ class Net:
         need = max(self.tc.wgrad_bf16_workspace_size(d["s"]) for d in self.L)
         if need > self.ws.numel() * 4:
             self.ws = self.torch.empty(need // 4 + 1, device="cuda")
+        self.ws2 = self.ws   # the step's weight gradients run one at a time on the side stream
 
     def step_bf16(self):
-        """One BF16 step: weight preparation, forward, input gradient, weight gradient of every layer."""
-        for fam in ("prep", "fwd", "dgrad", "wgrad"):
-            self.step_family(fam)
+        """One BF16 step: weight preparation, forward, input gradient, weight gradient of every layer,
+        scheduled as a training step's dependencies allow on two streams:
+          forward  -- the layer chain; a first block's downsample convolution (same input as its
+                      conv1) runs beside conv1..conv3 and joins before the next block;
+          backward -- the input-gradient chain in reverse layer order on the main stream; the weight
+                      gradient of layer i on the second stream as soon as dY_i exists (after the input
+                      gradient of layer i+1; the last layer's at once)."""
+        torch, tc, cg = self.torch, self.tc, self.cg
+        main, side = torch.cuda.current_stream(), self.side
+        self.prep.launch(main)
+        blk = None
+        for d in self.L:
+            s, name = d["s"], self.layers[d["i"]]["name"]
+            if name.endswith("_conv1"):
+                blk = torch.cuda.Event()
+                blk.record(main)
+            st = main
+            if name.endswith("_down"):
+                side.wait_event(blk)
+                st = side
+            tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"], stream=st)
+            if st is side:
+                main.wait_stream(side)
+        ready = torch.cuda.Event()
+        ready.record(main)
+        for d in reversed(self.L):
+            s = d["s"]
+            side.wait_event(ready)
+            tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], self.ws2, stream=side)
+            if not d["first"]:
+                tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"], stream=main)
+                ready = torch.cuda.Event()
+                ready.record(main)
+        main.wait_stream(side)
 
     def step_family(self, fam):
         """Launches one kernel family of the BF16 step; returns how many kernels it launched."""
@@ -1065,9 +1113,24 @@ def main():
                "wgrad": "tc_wgrad_kernel + wgrad_reduce_kernel"}
     dominant = max(("fwd", "dgrad", "wgrad"), key=lambda k: fam_summary[k]["ms"])
     dom = fam_summary[dominant]
+    # algorithmic bytes of the family per step: X, dY (or W) read, output written once
+    alg_bytes = 0
+    for d, l in zip(net.L, layers):
+        if dominant == "dgrad" and d["first"]:
+            continue
+        ho, wo = out_hw(l)
+        xb, yb = 2 * batch * l["h"] * l["w"] * c8(l["c"]), 2 * batch * ho * wo * l["kn"]
+        wb = l["c"] * l["k"] * l["k"] * l["kn"]
+        alg_bytes += xb + yb + wb * (4 if dominant == "wgrad" else 2)
+    traffic = profile_traffic(("tc_wgrad_kernel", "wgrad_reduce_kernel", "wgrad_group_sum_kernel")) \
+        if dominant == "wgrad" else None
     roofline = {"bound": "tensor", "kernel": kern_of[dominant], "achieved": dom["tflops"],
                 "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
-                "frac": dom["tflops"] / peaks["bf16_tflops_sustained"], "traffic": None,
+                "frac": dom["tflops"] / peaks["bf16_tflops_sustained"], "traffic": traffic,
+                "traffic_unit": "bytes per step of the family",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step's launches, "
+                                  "profiles/launches_resnet50_bf16_b64.md (cold cache between launches)",
+                "algorithmic_bytes": alg_bytes,
                 "peak_source": f"{peak_kind} bf16_tflops_sustained (kernel timed inside a long step)",
                 "how": "each kernel family of the step captured as its own CUDA graph, replayed, CUDA events; "
                        "achieved = algorithmic FLOPs (2*b*ho*wo*kn*c*kh*kw per conv) / device time",
@@ -1133,6 +1196,9 @@ def main():
                                        "+ weight grad, NHWC, BF16 tcgen05, FP32 accumulate",
                            "global_batch": batch * world, "per_gpu_batch": batch, "seq_len": None,
                            "parallelism": f"replicas{world}", "step": "one CUDA graph replay",
+                           "schedule": "two streams: forward chain with each downsample conv beside its block; "
+                                       "backward dgrad chain on one stream, wgrad of layer i on the other once "
+                                       "dY_i exists",
                            "l2": "inputs larger than L2 (per-step working set of several GB)",
                            "gflop_per_img": flops / batch / 1e9,
                            "autotune": tune_stats, "autotune_s": tune_s},

@@ -29,6 +29,7 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
+OP_CACHE_TAG = "mt"   # op entries measured with the M-tile choice
 
 
 def cache_path() -> str:
@@ -145,7 +146,7 @@ OP_NAMES = {tc.TUNE_FWD: "fwd", tc.TUNE_DGRAD: "dgrad", tc.TUNE_WGRAD: "wgrad", 
 
 
 def op_key(op: int, s) -> str:
-    return f"{OP_NAMES[op]}|{shape_key(s)}"
+    return f"{OP_NAMES[op]}.{OP_CACHE_TAG}|{shape_key(s)}"
 
 
 def graph_time_us(run, reps: int = 10) -> float:
@@ -171,9 +172,12 @@ def graph_time_us(run, reps: int = 10) -> float:
 
 
 def op_candidates(op: int, s):
-    """(bn, splits) candidates; splits 0 = heuristic (only the weight gradient varies it)."""
-    if op == tc.TUNE_DGRAD:
-        return [(w, 0) for w in candidate_widths(s.c)]
+    """(bn, aux) candidates: aux = weight-gradient pixel splits, or M tiles (1 / 2) sharing each
+    weight tile of the BF16 forward / input gradient; 0 = heuristic."""
+    if op == tc.TUNE_DGRAD:   # second value: M tiles sharing a weight tile
+        return [(w, m) for w in candidate_widths(s.c) for m in (1, 2)]
+    if op == tc.TUNE_FWD:
+        return [(w, m) for w in candidate_widths(s.kn) for m in (1, 2)]
     if op != tc.TUNE_WGRAD:
         return [(w, 0) for w in candidate_widths(s.kn)]
     tc.tune_set(op, s, 0, 0)

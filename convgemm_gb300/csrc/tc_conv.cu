@@ -45,7 +45,10 @@ constexpr int MODE_X3 = 2;    // 3xBF16: hi*hi + hi*lo + lo*hi into one accumula
 // KB 64-deep K blocks per pipeline stage: one full barrier and one MMA commit
 // cover KB blocks (a barrier round trip costs ~400 cycles, a 128 x 64 x 64 block
 // of BF16 MMAs ~150).
-template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16>
+// MT 128-row M tiles share every weight tile: each K block loads MT activation
+// tiles and one weight tile and issues MT MMAs into MT accumulators, which cuts
+// the shared-memory bytes per FLOP (the operand delivery from L2 bounds the kernel).
+template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16, int MT = 1>
 struct TcCfg {
     static constexpr int BM = 128, BK = 64;            // K elements per block
     static constexpr int ROWB = MODE == MODE_FP8 ? 64 : 128;  // bytes of one K row of a block
@@ -54,7 +57,7 @@ struct TcCfg {
     static constexpr uint32_t B_TILE = BN * ROWB;
     static constexpr uint32_t A_BLOCK = NOPS * A_TILE;
     static constexpr uint32_t B_BLOCK = NOPS * B_TILE;
-    static constexpr uint32_t A_BYTES = KB * A_BLOCK;
+    static constexpr uint32_t A_BYTES = KB * MT * A_BLOCK;
     static constexpr uint32_t B_BYTES = KB * B_BLOCK;
     static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t SBO = 8 * ROWB;                  // 8-row swizzle atom
@@ -73,6 +76,9 @@ struct TcCfg {
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + EPI_BUFS * EPI_BYTES + 256 + TAB_BYTES;
     static_assert(SMEM <= 232448, "shared memory above the 227 KB per-block limit");
     static constexpr int THREADS = 288;
+    // TMEM: MT accumulators of BN columns, double-buffered when 512 columns allow
+    static constexpr int ACC_BUFS = 2 * BN * MT <= 512 ? 2 : 1;
+    static constexpr uint32_t TMEM_COLS = ACC_BUFS * BN * MT;
 };
 
 __device__ __forceinline__ uint64_t op_desc(uint32_t saddr, uint32_t sbo, uint32_t layout) {
@@ -113,23 +119,24 @@ struct ClsS {
 };
 static_assert(sizeof(ClsS) <= 128, "class table entry");
 
-__device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntiles, int bn, int t) {
+__device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntiles, int bn, int t, int mt = 1) {
     int c = 0;
     while (c + 1 < ncls && t >= cls[c + 1].tile0) c++;
     const int local = t - cls[c].tile0;
     Tile tl;
     tl.cls = c;
-    tl.m0 = (local / ntiles) * 128;
+    tl.m0 = (local / ntiles) * 128 * mt;
     tl.n0 = (local % ntiles) * bn;
     return tl;
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT>
 __global__ void __launch_bounds__(288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
-    using C = TcCfg<BN, STAGES, KB, MODE>;
+    using C = TcCfg<BN, STAGES, KB, MODE, MT>;
     static_assert(IM2C || (KB == 1 && MODE == MODE_BF16), "the cp.async gather fills one BF16 K block per stage");
+    static_assert(MT == 1 || (IM2C && MODE == MODE_BF16), "two M tiles per weight tile: BF16 im2col path only");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *epi_smem = base + STAGES * C::STAGE_BYTES;
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(288, 1)
             sh_tab[n] = p.shift ? __ldg(p.shift + n) : 0.0f;
         }
     if (warp == 8) {
-        tc::tmem_alloc(tmem_holder, 2 * BN);
+        tc::tmem_alloc(tmem_holder, C::TMEM_COLS);
         tc::tmem_relinquish();
     }
     tc::tc_fence_before();
@@ -199,14 +206,20 @@ __global__ void __launch_bounds__(288, 1)
         if (threadIdx.x == 0) {
             uint32_t it = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
-                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile, MT);
                 const ClsS &cl = cls_tab[tl.cls];
                 const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
                 const int ktiles = cl.ktiles, kbeg = cl.kbeg, mint_y = cl.mint_y, mint_x = cl.mint_x;
-                uint32_t q, jw, j, b;
-                cl.dwg.divmod(tl.m0, q, jw);
-                cl.dhg.divmod(q, b, j);
-                const int h0 = (int) j * cl.isy + cl.lo_y, w0 = (int) jw * cl.isx + cl.lo_x;
+                int h0[MT], w0[MT], bb0[MT];   // im2col start of each M tile (beyond the class: zero-filled)
+#pragma unroll
+                for (int mt = 0; mt < MT; mt++) {
+                    uint32_t q, jw, j, b;
+                    cl.dwg.divmod(tl.m0 + mt * 128, q, jw);
+                    cl.dhg.divmod(q, b, j);
+                    h0[mt] = (int) j * cl.isy + cl.lo_y;
+                    w0[mt] = (int) jw * cl.isx + cl.lo_x;
+                    bb0[mt] = (int) b;
+                }
                 const CUtensorMap *am = &amaps.a[tl.cls];
                 int tap = 0, ci0 = 0;   // k = tap*Cin + ci0, walked incrementally
                 for (int kt = 0; kt < ktiles; kt += KB, it++) {
@@ -215,18 +228,21 @@ __global__ void __launch_bounds__(288, 1)
                     if (it >= (uint32_t) STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 1))) break;
                     const int nkb = min(KB, ktiles - kt);
                     const uint32_t sa = tc::smem_u32(base + s * C::STAGE_BYTES);
-                    tc::mbar_arrive_expect_tx(&full[s], nkb * (C::A_BLOCK + C::B_BLOCK));
+                    tc::mbar_arrive_expect_tx(&full[s], nkb * (MT * C::A_BLOCK + C::B_BLOCK));
                     for (int kb = 0; kb < nkb; kb++) {
                         const int32_t to = taps[tap];
                         const uint16_t offy = (uint16_t) ((to >> 16) - mint_y);
                         const uint16_t offx = (uint16_t) ((int32_t) (int16_t) (to & 0xFFFF) - mint_x);
-                        const uint32_t ab = sa + kb * C::A_BLOCK, bb = sa + C::A_BYTES + kb * C::B_BLOCK;
+                        const uint32_t ab = sa + kb * MT * C::A_BLOCK, bb = sa + C::A_BYTES + kb * C::B_BLOCK;
                         const int kcol = kbeg + (kt + kb) * C::BK;
-                        tc::tma_load_im2col_4d(ab, am, ci0, w0, h0, (int) b, offx, offy, &full[s]);
+#pragma unroll
+                        for (int mt = 0; mt < MT; mt++)
+                            tc::tma_load_im2col_4d(ab + mt * C::A_BLOCK, am, ci0, w0[mt], h0[mt], bb0[mt], offx, offy,
+                                                   &full[s]);
                         tc::tma_load_2d(bb, &wmap, kcol, tl.n0, &full[s]);
                         if (MODE == MODE_X3) {
-                            tc::tma_load_im2col_4d(ab + C::A_TILE, &amaps.alo[tl.cls], ci0, w0, h0, (int) b, offx, offy,
-                                                   &full[s]);
+                            tc::tma_load_im2col_4d(ab + C::A_TILE, &amaps.alo[tl.cls], ci0, w0[0], h0[0], bb0[0], offx,
+                                                   offy, &full[s]);
                             tc::tma_load_2d(bb + C::B_TILE, &amaps.wlo, kcol, tl.n0, &full[s]);
                         }
                         ci0 += 64;
@@ -311,10 +327,10 @@ __global__ void __launch_bounds__(288, 1)
         uint32_t lt = 0;                  // local tile count
         int ebuf = 0;                     // staging buffer toggle
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
-            const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+            const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile, MT);
             const ClsS &cl = cls_tab[tl.cls];
             const int M = p.B * cl.Hg * cl.Wg;
-            const int buf = lt & 1;
+            const int buf = lt % C::ACC_BUFS;
             const float *scp = sc_tab, *shp = sh_tab;
             if (sc_all) {
                 scp += tl.n0;
@@ -329,10 +345,13 @@ __global__ void __launch_bounds__(288, 1)
                 }
                 epi_bar();
             }
-            ok = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 3);
+            ok = tc::mbar_wait(&acc_full[buf], (lt / C::ACC_BUFS) & 1, p.err, 3);
             if (!ok) break;
             tc::tc_fence_after();
-            const int m = tl.m0 + row;
+#pragma unroll 1
+          for (int mt = 0; mt < MT; mt++) {
+            const int m0 = tl.m0 + mt * 128;   // this accumulator's first output row
+            const int m = m0 + row;
             uint8_t *orow = nullptr;   // this row of the output (BF16, or FP32 for MODE_X3)
             if (!p.epi_tma && m < M) {
                 uint32_t q, jw, j, b;
@@ -344,11 +363,11 @@ __global__ void __launch_bounds__(288, 1)
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += C::CW) {
                 uint32_t v0[32], v1[32];
-                const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) (buf * BN + c0);
+                const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) ((buf * MT + mt) * BN + c0);
                 tc::tmem_ld_32x32b_x32(ta, v0);
                 if (C::CW == 64) tc::tmem_ld_32x32b_x32(ta + 32, v1);
                 tc::tmem_ld_wait();
-                if (c0 + C::CW >= BN) {
+                if (mt == MT - 1 && c0 + C::CW >= BN) {
                     // the whole accumulator is in registers: hand the TMEM buffer back to the MMA warp
                     tc::tc_fence_before();
                     tc::mbar_arrive(&acc_empty[buf]);
@@ -384,8 +403,8 @@ __global__ void __launch_bounds__(288, 1)
                     }
                     tc::fence_proxy_async_smem();
                     __syncwarp();
-                    if (lane == 0 && nb < p.Cout && tl.m0 + ew * 32 < M) {
-                        tma_store_2d(&omap, tc::smem_u32(stg), nb, tl.m0 + ew * 32);
+                    if (lane == 0 && nb < p.Cout && m0 + ew * 32 < M) {
+                        tma_store_2d(&omap, tc::smem_u32(stg), nb, m0 + ew * 32);
                         bulk_commit();
                     }
                     if (C::EPI_BUFS == 2) ebuf ^= 1;
@@ -410,6 +429,7 @@ __global__ void __launch_bounds__(288, 1)
                     }
                 }
             }
+          }
         }
         if (lane == 0) bulk_wait_all();
     } else {
@@ -418,15 +438,15 @@ __global__ void __launch_bounds__(288, 1)
             constexpr uint32_t idesc = MODE == MODE_FP8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, BN, 0, 0);
             uint32_t it = 0, lt = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
-                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
+                const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile, MT);
                 const int KT = cls_tab[tl.cls].ktiles;
-                const int buf = lt & 1;
-                if (lt >= 2) {
-                    ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) - 1) & 1, p.err, 4);
+                const int buf = lt % C::ACC_BUFS;
+                if (lt >= (uint32_t) C::ACC_BUFS) {
+                    ok = tc::mbar_wait(&acc_empty[buf], ((lt / C::ACC_BUFS) - 1) & 1, p.err, 4);
                     if (!ok) break;
                     tc::tc_fence_after();
                 }
-                const uint32_t dt = tmem + (uint32_t) (buf * BN);
+                const uint32_t dt = tmem + (uint32_t) (buf * MT * BN);
                 for (int kt = 0; kt < KT; kt += KB, it++) {
                     const int s = it % STAGES;
                     const uint32_t ph = (it / STAGES) & 1;
@@ -439,24 +459,29 @@ __global__ void __launch_bounds__(288, 1)
                     const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
                     const uint32_t b0 = a0 + C::A_BYTES;
                     for (int kb = 0; kb < nkb; kb++) {
-                        const uint32_t ab = a0 + kb * C::A_BLOCK, bb = b0 + kb * C::B_BLOCK;
+                        const uint32_t bb = b0 + kb * C::B_BLOCK;
                         // each MMA consumes 32 bytes of every K row: 16 BF16 or 32 E4M3 elements
 #pragma unroll
                         for (int k = 0; k < C::ROWB / 32; k++) {
                             const uint32_t acc = (kt | kb | k) != 0;
-                            const uint64_t ad = op_desc(ab + k * 32, C::SBO, C::LAYOUT);
                             const uint64_t bd = op_desc(bb + k * 32, C::SBO, C::LAYOUT);
+#pragma unroll
+                          for (int mt = 0; mt < MT; mt++) {
+                            const uint32_t ab = a0 + (kb * MT + mt) * C::A_BLOCK;
+                            const uint64_t ad = op_desc(ab + k * 32, C::SBO, C::LAYOUT);
+                            const uint32_t dtm = dt + (uint32_t) (mt * BN);
                             if (MODE == MODE_FP8) {
-                                tc::mma_f8(dt, ad, bd, idesc, acc);
+                                tc::mma_f8(dtm, ad, bd, idesc, acc);
                             } else {
-                                tc::mma_f16(dt, ad, bd, idesc, acc);
+                                tc::mma_f16(dtm, ad, bd, idesc, acc);
                                 if (MODE == MODE_X3) {
                                     const uint64_t adl = op_desc(ab + C::A_TILE + k * 32, C::SBO, C::LAYOUT);
                                     const uint64_t bdl = op_desc(bb + C::B_TILE + k * 32, C::SBO, C::LAYOUT);
-                                    tc::mma_f16(dt, ad, bdl, idesc, 1);   // hi * lo
-                                    tc::mma_f16(dt, adl, bd, idesc, 1);   // lo * hi
+                                    tc::mma_f16(dtm, ad, bdl, idesc, 1);   // hi * lo
+                                    tc::mma_f16(dtm, adl, bd, idesc, 1);   // lo * hi
                                 }
                             }
+                          }
                         }
                     }
                     tc::mma_commit(&empty[s]);
@@ -470,14 +495,14 @@ __global__ void __launch_bounds__(288, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 8) tc::tmem_dealloc(tmem, 2 * BN);
+    if (warp == 8) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT = 1>
 cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
                       int grid, cudaStream_t st) {
-    using C = TcCfg<BN, STAGES, KB, MODE>;
-    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE>;
+    using C = TcCfg<BN, STAGES, KB, MODE, MT>;
+    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE, MT>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -512,6 +537,16 @@ cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const
             default: return cudaErrorInvalidValue;
         }
     }
+    if (p.im2col && p.mt == 2) {
+        // two M tiles per weight tile: 40 / 48 / 64 KB per K block
+        switch (p.bn) {
+            case 64: return launch_bn<64, 4, 1, true, MODE_BF16, 2>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 4, 1, true, MODE_BF16, 2>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 1, true, MODE_BF16, 2>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (p.mt != 1) return cudaErrorInvalidValue;
     if (p.im2col) {
         switch (p.bn) {
             case 64: return launch_bn<64, 4, 2, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);

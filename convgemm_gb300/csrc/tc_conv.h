@@ -44,6 +44,7 @@ struct TcConvParams {
     int im2col;                // A loaded by im2col-mode TMA (Cin % 64 == 0), else gathered by cp.async
     int cpb;                   // 64-channel chunks per tap (Cin / 64) on the im2col path
     int mode;                  // 0 BF16, 1 FP8-E4M3, 2 3xBF16 (FP32 output)
+    int mt;                    // 128-row M tiles per tile (1, or 2 sharing each weight tile: BF16 im2col only)
     int ncls;
     TcClass cls[TC_MAXCLS];
 };

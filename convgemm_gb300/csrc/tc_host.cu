@@ -277,7 +277,7 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
-                         const void *in_lo, const void *w_lo, int bn_override) {
+                         const void *in_lo, const void *w_lo, int bn_override, int mt_override) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
     TcConvParams p;
@@ -345,11 +345,13 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
                     tc_make_map_2d(&amaps.wlo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, w_lo, pl.Cout, pl.Ktot, 64, p.bn))
                 return e;
     }
+    // two M tiles per weight tile only on the BF16 im2col path
+    p.mt = (mt_override == 2 && mode == 0 && p.im2col) ? 2 : 1;
     int t0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
         p.cls[c] = pi.cls[c];
         p.cls[c].tile0 = t0;
-        t0 += pl.cls[c].mtiles * p.ntiles;
+        t0 += (pl.cls[c].mtiles + p.mt - 1) / p.mt * p.ntiles;
     }
     p.ntiles_total = t0;
     const int grid = t0 < sms ? t0 : sms;
@@ -445,7 +447,8 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
     tc_plan_fwd(s, pl);
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_FWD, *shape, &t);
-    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 0, nullptr, nullptr, t.bn);
+    return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 0, nullptr, nullptr, t.bn,
+                  t.splits);
 }
 
 extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
@@ -466,7 +469,7 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, 
     }
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
-    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn);
+    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits);
 }
 
 // ------------------------------------------------------- weight gradient

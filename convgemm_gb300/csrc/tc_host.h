@@ -27,7 +27,9 @@ convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, i
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
 bool tc_plan_im2col(TcPlan &pl);
 int tc_num_sms();
-// Autotuned tile configuration of one operation on one shape (0 = heuristic).
+// Autotuned tile configuration of one operation on one shape (0 = heuristic):
+// bn = output channels per tile; splits = pixel splits of the weight gradient,
+// or M tiles per weight tile (1 or 2) of the forward / input gradient.
 struct TcTune {
     int bn, splits;
 };
@@ -36,4 +38,5 @@ bool tc_tune_get(int op, const convgemm_shape_t &s, TcTune *t);
 // mode: 0 BF16, 1 FP8-E4M3 (in/wpacked are E4M3), 2 3xBF16 (in_lo/w_lo low parts, FP32 output)
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,
-                         const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0);
+                         const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0,
+                         int mt_override = 0);

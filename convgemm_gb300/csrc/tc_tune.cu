@@ -34,8 +34,11 @@ extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *s
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: bad operation or NULL shape");
     if (bn != 0 && bn != 64 && bn != 128 && bn != 256)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: tile width %d is not 0/64/128/256", bn);
-    if (splits < 0 || (splits > 0 && op != CONVGEMM_TUNE_WGRAD))
-        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: splits apply to the weight gradient only");
+    const bool mt_op = op == CONVGEMM_TUNE_FWD || op == CONVGEMM_TUNE_DGRAD;
+    if (splits < 0 || (op != CONVGEMM_TUNE_WGRAD && splits > (mt_op ? 2 : 0)))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE,
+                            "convgemm_tune_set: aux is the weight gradient's split count, or 1/2 M tiles per weight "
+                            "tile of the BF16 forward / input gradient");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     if (bn == 0 && splits == 0)
         g_tune.erase(key_of(op, *shape));

@@ -206,11 +206,12 @@ enum {
 
 /* Process-wide override of the built-in heuristics for one operation on one
  * shape, as chosen by an autotuner: bn = output channels per tile (64, 128 or
- * 256; for the weight gradient the width of its N side), splits = pixel splits
- * of the weight gradient (0 = heuristic; weight gradient only).  bn = splits =
- * 0 removes the entry.  Set the weight-gradient entry before querying its
- * workspace size.  Thread-safe. */
-convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int splits);
+ * 256; for the weight gradient the width of its N side); aux = pixel splits of
+ * the weight gradient, or, for the BF16 forward / input gradient, the number of
+ * 128-row M tiles (1 or 2) that share each weight tile (0 = heuristic).
+ * bn = aux = 0 removes the entry.  Set the weight-gradient entry before querying
+ * its workspace size.  Thread-safe. */
+convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int aux);
 void convgemm_tune_clear(void);
 
 /* ----------------------------------------- grouped persistent forward launch */

@@ -185,8 +185,9 @@ def test_wgrad_bf16_rejects_small_workspace(cglib):
 
 
 def test_tuned_tile_configurations_agree(cglib, oracle_lib):
-    """Every tile width of the tuning table gives the same forward / input-gradient result
-    (the K order of an output does not depend on the tile width); every weight-gradient
+    """Every tile width and M-tile count of the tuning table gives the same forward /
+    input-gradient result (the K order of an output does not depend on them; 7 M tiles
+    leave the last pair with an empty tile); every weight-gradient
     split count stays within tolerance of FP64 and is reproducible."""
     from convgemm_gb300 import tc
     cg, O = cglib, oracle_lib
@@ -203,9 +204,9 @@ def test_tuned_tile_configurations_agree(cglib, oracle_lib):
     wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
     try:
         ys, dxs = [], []
-        for bn in (64, 128, 256):
-            tc.tune_set(tc.TUNE_FWD, s, bn)
-            tc.tune_set(tc.TUNE_DGRAD, s, bn)
+        for bn, mt in ((64, 1), (128, 1), (256, 1), (64, 2), (128, 2), (256, 2)):
+            tc.tune_set(tc.TUNE_FWD, s, bn, mt)
+            tc.tune_set(tc.TUNE_DGRAD, s, bn, mt)
             y = torch.empty(b, h, w, kn, dtype=torch.bfloat16, device="cuda")
             tc.fwd_bf16(s, xd, wp, y)
             dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
@@ -268,3 +269,38 @@ def test_grouped_preparation_matches_per_layer_calls(cglib):
         for k, v in want.items():
             assert torch.equal(it[k].view(torch.int16) if v.dtype == torch.bfloat16 else it[k],
                                v.view(torch.int16) if v.dtype == torch.bfloat16 else v), k
+
+
+def test_two_m_tiles_strided_input_gradient(cglib, oracle_lib):
+    """Stride-2 input gradient (4 stride-phase classes with odd M-tile counts) with two M tiles
+    per weight tile: identical to one M tile, and within tolerance of FP64."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn = 3, 15, 15, 128, 128
+    s = cg.Shape.of(b, h, w, c, kn, 3, 3, 1, 1, 2, 2)
+    g = C.geom(b, h, w, c, kn, 3, 3, pad=1, stride=2)
+    rng = np.random.default_rng(78)
+    wt = (rng.standard_normal(9 * c * kn) * np.sqrt(2.0 / (9 * c))).astype(np.float32)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
+    try:
+        outs = []
+        for mt in (1, 2):
+            tc.tune_set(tc.TUNE_DGRAD, s, 128, mt)
+            tc.tune_set(tc.TUNE_FWD, s, 128, mt)
+            dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
+            tc.dgrad_bf16(s, dyd, wpd, dx)
+            y = torch.empty(b, s.ho, s.wo, kn, dtype=torch.bfloat16, device="cuda")
+            tc.fwd_bf16(s, xd, wp, y)
+            outs.append((dx, y))
+        torch.cuda.synchronize()
+        cg.check_device()
+        assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+        ref = O.dgrad_f64(C.NHWC, g, wt, dy)
+        assert rel_max_rms(outs[1][0].float().cpu().numpy(), ref)[0] <= BF16_TOL
+    finally:
+        tc.tune_clear()
