@@ -26,6 +26,7 @@ convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, in
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
 bool tc_plan_im2col(TcPlan &pl);
+
 int tc_num_sms();
 // Autotuned tile configuration of one operation on one shape (0 = heuristic):
 // bn = output channels per tile; splits = pixel splits of the weight gradient,

@@ -47,6 +47,9 @@ FWD_SHAPES = [
     (1, 13, 11, 40, 72, 3, 2, 1, 2),     # ragged channels, dilation
     (2, 8, 8, 256, 1024, 1, 0, 1, 1),
     (1, 15, 15, 96, 192, 3, 1, 2, 1),
+    (1, 17, 19, 8, 72, 5, 2, 1, 1),      # small-channel path: 25 taps (7 padded), one 128-wide N tile for 72 channels
+    (2, 11, 9, 5, 64, 3, 1, 2, 2),       # small-channel path: stride 2, dilation 2
+    (3, 30, 30, 3, 128, 7, 3, 2, 1),     # small-channel path: stem with 128 output channels
 ]
 
 
