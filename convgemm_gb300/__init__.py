@@ -116,6 +116,12 @@ def lib():
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_launch_count.restype = ctypes.c_ulonglong
+        _HG = [_I] * 14
+        L.im2row_nhwc.argtypes = [_VP, _I, _VP] + _HG
+        L.im2col_nchw.argtypes = [_VP, _I, _VP] + _HG
+        L.row2im_nhwc.argtypes = [_I, _I, _VP, _I, _VP] + _HG
+        L.col2im_nchw.argtypes = [_I, _I, _VP, _I, _VP] + _HG
+        L.transpose_nchw.argtypes = [_I, _I, _VP, _I, ctypes.c_float, _VP, _I, _I, _I, _I, _I]
         L.convgemm_tune_set.argtypes = [_I, SP, _I, _I]
         L.convgemm_wgrad_bf16_plan.argtypes = [SP, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]
         L.convgemm_prep_table_size.argtypes = [_I]
@@ -131,6 +137,49 @@ def lib():
         L.convgemm_group_launch.argtypes = [_VP, _I, _I, _VP]
         _lib = L
     return _lib
+
+
+# ---------------------------------------------- explicit lowering helpers (drop-in)
+def _check_void():
+    st, msg = last_error()
+    if st:
+        lib().convgemm_clear_error()
+        raise ConvGemmError(st, msg)
+
+
+def im2row_nhwc(rows, ld, x, b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil):
+    """rows[(b,x,y)][(c,kx,ky)] = x[b][ix][iy][c] (src/im2row_nhwc.c:147-170)."""
+    lib().convgemm_clear_error()
+    lib().im2row_nhwc(ptr(rows), ld, ptr(x), b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)
+    _check_void()
+
+
+def row2im_nhwc(m, n, rows, ld, out, b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil):
+    """out[b][ix][iy][c] += rows[...] (src/im2row_nhwc.c:210-229)."""
+    lib().convgemm_clear_error()
+    lib().row2im_nhwc(m, n, ptr(rows), ld, ptr(out), b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)
+    _check_void()
+
+
+def im2col_nchw(cols, ld, x, b, c, h, w, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil):
+    """cols[(c,kx,ky)][(b,x,y)] = x[b][c][ix][iy] (src/im2col_nchw.c:146-170)."""
+    lib().convgemm_clear_error()
+    lib().im2col_nchw(ptr(cols), ld, ptr(x), b, c, h, w, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)
+    _check_void()
+
+
+def col2im_nchw(m, n, cols, ld, out, b, c, h, w, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil):
+    """out[b][c][ix][iy] += cols[...] (src/im2col_nchw.c:337-359)."""
+    lib().convgemm_clear_error()
+    lib().col2im_nchw(m, n, ptr(cols), ld, ptr(out), b, c, h, w, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)
+    _check_void()
+
+
+def transpose_nchw(rows, cols, x, ld, beta, out, kn, ho, wo, start_row, start_col):
+    """out[b][start_col + j][x][y] = x[j*ld + i] (+ beta*out) (src/im2col_nchw.c:208-233)."""
+    lib().convgemm_clear_error()
+    lib().transpose_nchw(rows, cols, ptr(x), ld, beta, ptr(out), kn, ho, wo, start_row, start_col)
+    _check_void()
 
 
 def launch_count() -> int:

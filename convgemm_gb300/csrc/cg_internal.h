@@ -37,3 +37,15 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
 int *cg_device_error_word();
 // Counts one kernel launch made by the library (convgemm_launch_count).
 void cg_note_launch();
+
+// Explicit lowering helpers (cg_helpers.cu), device pointers.
+cudaError_t cg_helper_im2row(float *rows, const float *in, int b, int h, int w, int c, int ho, int wo, int kh, int kw,
+                             int vpad, int hpad, int vstr, int hstr, int vdil, int hdil, cudaStream_t st);
+cudaError_t cg_helper_row2im(const float *rows, float *out, int b, int h, int w, int c, int ho, int wo, int kh, int kw,
+                             int vpad, int hpad, int vstr, int hstr, int vdil, int hdil, cudaStream_t st);
+cudaError_t cg_helper_im2col(float *cols, const float *in, int b, int c, int h, int w, int ho, int wo, int kh, int kw,
+                             int vpad, int hpad, int vstr, int hstr, int vdil, int hdil, cudaStream_t st);
+cudaError_t cg_helper_col2im(const float *cols, float *out, int b, int c, int h, int w, int ho, int wo, int kh, int kw,
+                             int vpad, int hpad, int vstr, int hstr, int vdil, int hdil, cudaStream_t st);
+cudaError_t cg_helper_transpose(int rows, int cols, const float *in, int ld, float beta, float *out, int kn, int ho,
+                                int wo, int start_row, int start_col, cudaStream_t st);

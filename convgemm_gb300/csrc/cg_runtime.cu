@@ -334,6 +334,125 @@ void dropin_back(int nchw, const convgemm_shape_t &s, const float *weights, cons
 
 }  // namespace
 
+// ------------------------------------------- explicit lowering helpers (drop-in)
+// The reference's im2row_nhwc / row2im_nhwc / im2col_nchw / col2im_nchw /
+// transpose_nchw (src/im2row_nhwc.h:20-29, src/im2col_nchw.h:20-38) on the GPU,
+// with the same staging of host pointers as the convolution entry points.
+namespace {
+
+bool helper_geom_ok(const char *fn, int b, int h, int w, int c, int ho, int wo, int kh, int kw, int vpad, int hpad,
+                    int vstr, int hstr, int vdil, int hdil) {
+    if (b < 1 || h < 1 || w < 1 || c < 1 || ho < 1 || wo < 1 || kh < 1 || kw < 1 || vpad < 0 || hpad < 0 ||
+        vstr < 1 || hstr < 1 || vdil < 1 || hdil < 1) {
+        cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: invalid geometry", fn);
+        return false;
+    }
+    return true;
+}
+
+// in -> lowered (im2row / im2col); the lowered buffer is read too: padding entries stay as they were
+void helper_lower(bool nchw, float *low, const float *in, int b, int h, int w, int c, int ho, int wo, int kh, int kw,
+                  int vpad, int hpad, int vstr, int hstr, int vdil, int hdil) {
+    const char *fn = nchw ? "im2col_nchw" : "im2row_nhwc";
+    if (!helper_geom_ok(fn, b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)) return;
+    if (!low || !in) {
+        cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL tensor", fn);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    Arg a_low{low, nullptr, sizeof(float) * (size_t) b * ho * wo * c * kh * kw, false};
+    Arg a_in{in, nullptr, sizeof(float) * (size_t) b * h * w * c, false};
+    if (!stage_in(a_in, SLOT_IN, true) || !stage_in(a_low, SLOT_OUT, true)) return;
+    cudaError_t e = nchw ? cg_helper_im2col((float *) a_low.dev, (const float *) a_in.dev, b, c, h, w, ho, wo, kh, kw,
+                                            vpad, hpad, vstr, hstr, vdil, hdil, 0)
+                         : cg_helper_im2row((float *) a_low.dev, (const float *) a_in.dev, b, h, w, c, ho, wo, kh, kw,
+                                            vpad, hpad, vstr, hstr, vdil, hdil, 0);
+    if (cg_cuda_check(e, fn)) return;
+    if (a_low.staged) stage_out(a_low);
+}
+
+// lowered -> out, accumulated (row2im / col2im)
+void helper_raise(bool nchw, const float *low, float *out, int b, int h, int w, int c, int ho, int wo, int kh, int kw,
+                  int vpad, int hpad, int vstr, int hstr, int vdil, int hdil) {
+    const char *fn = nchw ? "col2im_nchw" : "row2im_nhwc";
+    if (!helper_geom_ok(fn, b, h, w, c, ho, wo, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil)) return;
+    if (!low || !out) {
+        cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL tensor", fn);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    Arg a_low{low, nullptr, sizeof(float) * (size_t) b * ho * wo * c * kh * kw, false};
+    Arg a_out{out, nullptr, sizeof(float) * (size_t) b * h * w * c, false};
+    if (!stage_in(a_low, SLOT_IN, true) || !stage_in(a_out, SLOT_OUT, true)) return;
+    cudaError_t e = nchw ? cg_helper_col2im((const float *) a_low.dev, (float *) a_out.dev, b, c, h, w, ho, wo, kh, kw,
+                                            vpad, hpad, vstr, hstr, vdil, hdil, 0)
+                         : cg_helper_row2im((const float *) a_low.dev, (float *) a_out.dev, b, h, w, c, ho, wo, kh, kw,
+                                            vpad, hpad, vstr, hstr, vdil, hdil, 0);
+    if (cg_cuda_check(e, fn)) return;
+    if (a_out.staged) stage_out(a_out);
+}
+
+}  // namespace
+
+extern "C" void im2row_nhwc(float *rows, int ld, const float *in, int batches, int height, int width, int channels,
+                            int oheight, int owidth, int kheight, int kwidth, int vpadding, int hpadding, int vstride,
+                            int hstride, int vdilation, int hdilation) {
+    (void) ld;   // the reference's active branch uses rows of channels*kheight*kwidth (im2row_nhwc.c:157-164)
+    helper_lower(false, rows, in, batches, height, width, channels, oheight, owidth, kheight, kwidth, vpadding,
+                 hpadding, vstride, hstride, vdilation, hdilation);
+}
+
+extern "C" void row2im_nhwc(int m, int n, const float *rows, int ld, float *out, int batches, int height, int width,
+                            int channels, int oheight, int owidth, int kheight, int kwidth, int vpadding, int hpadding,
+                            int vstride, int hstride, int vdilation, int hdilation) {
+    (void) m, (void) n, (void) ld;   // as in the reference (im2row_nhwc.c:210-229)
+    helper_raise(false, rows, out, batches, height, width, channels, oheight, owidth, kheight, kwidth, vpadding,
+                 hpadding, vstride, hstride, vdilation, hdilation);
+}
+
+extern "C" void im2col_nchw(float *cols, int ld, const float *in, int batches, int channels, int height, int width,
+                            int oheight, int owidth, int kheight, int kwidth, int vpadding, int hpadding, int vstride,
+                            int hstride, int vdilation, int hdilation) {
+    (void) ld;   // the reference's active branch uses rows of batches*oheight*owidth (im2col_nchw.c:151-166)
+    helper_lower(true, cols, in, batches, height, width, channels, oheight, owidth, kheight, kwidth, vpadding,
+                 hpadding, vstride, hstride, vdilation, hdilation);
+}
+
+extern "C" void col2im_nchw(int m, int n, const float *cols, int ld, float *out, int batches, int channels, int height,
+                            int width, int oheight, int owidth, int kheight, int kwidth, int vpadding, int hpadding,
+                            int vstride, int hstride, int vdilation, int hdilation) {
+    (void) m, (void) n, (void) ld;   // as in the reference (im2col_nchw.c:337-359)
+    helper_raise(true, cols, out, batches, height, width, channels, oheight, owidth, kheight, kwidth, vpadding,
+                 hpadding, vstride, hstride, vdilation, hdilation);
+}
+
+extern "C" void transpose_nchw(int rows, int cols, const float *in, int ld, float beta, float *out, int kn, int ho,
+                               int wo, int start_row, int start_col) {
+    const char *fn = "transpose_nchw";
+    if (rows < 0 || cols < 0 || ld < rows || kn < 1 || ho < 1 || wo < 1 || start_row < 0 || start_col < 0 ||
+        start_col + cols > kn) {
+        cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: invalid arguments", fn);
+        return;
+    }
+    if (rows == 0 || cols == 0) return;
+    if (!in || !out) {
+        cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL tensor", fn);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    // extents: in[(cols-1)*ld + rows], out up to the last image the rows reach
+    const long long last_b = ((long long) start_row + rows - 1) / ((long long) ho * wo);
+    Arg a_in{in, nullptr, sizeof(float) * ((size_t) (cols - 1) * ld + rows), false};
+    Arg a_out{out, nullptr, sizeof(float) * (size_t) ((last_b + 1) * kn * ho * wo), false};
+    // out is copied in whole: the transpose writes only the entries of its rows and columns
+    if (!stage_in(a_in, SLOT_IN, true) || !stage_in(a_out, SLOT_OUT, true)) return;
+    if (cg_cuda_check(cg_helper_transpose(rows, cols, (const float *) a_in.dev, ld, beta, (float *) a_out.dev, kn, ho,
+                                          wo, start_row, start_col, 0),
+                      fn))
+        return;
+    if (a_out.staged) stage_out(a_out);
+}
+
 extern "C" int alloc_pack_buffs(float **Ac_pack, float **Bc_pack) {
     if (Ac_pack) *Ac_pack = nullptr;
     if (Bc_pack) *Bc_pack = nullptr;
