@@ -29,7 +29,7 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
-OP_CACHE_TAG = "mt"   # op entries measured with the M-tile choice
+OP_CACHE_TAG = "v3"   # op entries: fwd / dgrad with the M-tile choice, wgrad with 2-chunk stages and direct single-split writes
 
 
 def cache_path() -> str:

@@ -25,12 +25,16 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-template <int BN, int STAGES, bool XA>
+// KB chunks of BK pixels per pipeline stage: one full barrier and one MMA commit
+// cover KB chunks (the barrier round trip, not the loads or the MMAs, bounds a
+// one-chunk stage).
+template <int BN, int STAGES, bool XA, int KB = 1>
 struct WgCfg {
-    static constexpr int BM = 128, BK = 64;  // BK pixels per stage
+    static constexpr int BM = 128, BK = 64;  // BK pixels per chunk
     static constexpr uint32_t A_BYTES = BM * BK * 2;
     static constexpr uint32_t B_BYTES = BN * BK * 2;
-    static constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+    static constexpr uint32_t CHUNK_BYTES = A_BYTES + B_BYTES;
+    static constexpr uint32_t STAGE_BYTES = KB * CHUNK_BYTES;
     static constexpr int X_ATOMS = (XA ? BM : BN) / 64;    // 64-channel atoms gathered from X
     static constexpr int DY_ATOMS = (XA ? BN : BM) / 64;   // 64-channel atoms loaded from dY
     static constexpr uint32_t DY_BYTES = DY_ATOMS * 64 * BK * 2;
@@ -38,11 +42,12 @@ struct WgCfg {
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
 };
 
-template <int BN, int STAGES, bool XA, bool IM2C>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB>
 __global__ void __launch_bounds__(160, 1)
     tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
                     const __grid_constant__ CUtensorMap xmap) {
-    using C = WgCfg<BN, STAGES, XA>;
+    using C = WgCfg<BN, STAGES, XA, KB>;
+    static_assert(IM2C || KB == 1, "the cp.async gather fills one chunk per stage");
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint64_t *full = (uint64_t *) (base + STAGES * C::STAGE_BYTES);
@@ -75,7 +80,8 @@ __global__ void __launch_bounds__(160, 1)
     const int x0 = XA ? mrow0 : ncol0;
     const int co0 = XA ? ncol0 : mrow0;
     const int chunk0 = blockIdx.z * p.chunks_per_split;
-    const int KT = min(p.chunks_per_split, p.nchunks - chunk0);
+    const int KT = min(p.chunks_per_split, p.nchunks - chunk0);   // chunks of this split
+    const int NG = (KT + KB - 1) / KB;                              // pipeline stages they fill
     bool ok = true;
 
     if (IM2C && warp < 4) {
@@ -95,24 +101,27 @@ __global__ void __launch_bounds__(160, 1)
             }
             const uint32_t xoff = XA ? 0 : C::A_BYTES;
             const uint32_t dyoff = XA ? C::A_BYTES : 0;
-            for (int kt = 0; kt < KT; kt++) {
-                const int s = kt % STAGES;
-                const uint32_t ph = (kt / STAGES) & 1;
-                if (kt >= STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11))) break;
-                const int pbase = (chunk0 + kt) * C::BK;
-                uint32_t q, ow, oh, b;
-                p.dwo.divmod(pbase, q, ow);
-                p.dho.divmod(q, b, oh);
-                const int h0 = (int) oh * p.vstr - p.vpad, w0 = (int) ow * p.hstr - p.hpad;
-                const uint32_t st0 = tc::smem_u32(base + s * C::STAGE_BYTES);
-                tc::mbar_arrive_expect_tx(&full[s], C::X_ATOMS * 8192 + C::DY_BYTES);
+            for (int g = 0; g < NG; g++) {
+                const int s = g % STAGES;
+                const uint32_t ph = (g / STAGES) & 1;
+                if (g >= STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11))) break;
+                const int nch = min(KB, KT - g * KB);
+                tc::mbar_arrive_expect_tx(&full[s], nch * (C::X_ATOMS * 8192 + C::DY_BYTES));
+                for (int c = 0; c < nch; c++) {
+                    const int pbase = (chunk0 + g * KB + c) * C::BK;
+                    uint32_t q, ow, oh, b;
+                    p.dwo.divmod(pbase, q, ow);
+                    p.dho.divmod(q, b, oh);
+                    const int h0 = (int) oh * p.vstr - p.vpad, w0 = (int) ow * p.hstr - p.hpad;
+                    const uint32_t st0 = tc::smem_u32(base + s * C::STAGE_BYTES + c * C::CHUNK_BYTES);
 #pragma unroll
-                for (int a = 0; a < C::X_ATOMS; a++)
-                    tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a], a_oy[a],
-                                           &full[s]);
+                    for (int a = 0; a < C::X_ATOMS; a++)
+                        tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
+                                               a_oy[a], &full[s]);
 #pragma unroll
-                for (int a = 0; a < C::DY_ATOMS; a++)
-                    tc::tma_load_2d(st0 + dyoff + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
+                    for (int a = 0; a < C::DY_ATOMS; a++)
+                        tc::tma_load_2d(st0 + dyoff + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
+                }
             }
         }
         // epilogue below runs on all four warps
@@ -189,7 +198,29 @@ __global__ void __launch_bounds__(160, 1)
         const int m = mrow0 + warp * 32 + lane;
         const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx;
         float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
-        if (ok) {
+        if (ok && p.direct) {
+            // single split: dW written in the reference layout (lanes hold consecutive rows)
+            const int khw = p.kh * p.kw;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t v[32];
+                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+                tc::tmem_ld_wait();
+                if (m >= Mext) continue;
+#pragma unroll 4
+                for (int jj = 0; jj < 32; jj++) {
+                    const int col = ncol0 + c0 + jj;
+                    if (col >= Next) break;
+                    const int n = XA ? m : col, co = XA ? col : m;
+                    uint32_t tap, ci;
+                    p.dcp.divmod((uint32_t) n, tap, ci);
+                    if ((int) ci >= p.C) continue;
+                    const size_t o = p.layout == 0 ? ((size_t) ci * khw + tap) * p.kn + co
+                                                   : ((size_t) co * p.C + ci) * khw + tap;
+                    p.dw[o] = __uint_as_float(v[jj]);
+                }
+            }
+        } else if (ok) {
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t v[32];
@@ -214,21 +245,24 @@ __global__ void __launch_bounds__(160, 1)
     } else {
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
-            for (int kt = 0; kt < KT; kt++) {
-                const int s = kt % STAGES;
-                const uint32_t ph = (kt / STAGES) & 1;
+            for (int g = 0; g < NG; g++) {
+                const int s = g % STAGES;
+                const uint32_t ph = (g / STAGES) & 1;
                 if (!tc::mbar_wait(&full[s], ph, p.err, 12)) {
                     ok = false;
                     break;
                 }
                 tc::tc_fence_after();
-                const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
-                const uint32_t b0 = a0 + C::A_BYTES;
+                const int nch = min(KB, KT - g * KB);
+                for (int c = 0; c < nch; c++) {
+                    const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES + c * C::CHUNK_BYTES);
+                    const uint32_t b0 = a0 + C::A_BYTES;
 #pragma unroll
-                for (int k = 0; k < C::BK / 16; k++) {
-                    const uint64_t ad = tc::sw128_desc(a0 + k * 2048, 8192, 1024);
-                    const uint64_t bd = tc::sw128_desc(b0 + k * 2048, 8192, 1024);
-                    tc::mma_f16(tmem, ad, bd, idesc, (kt | k) != 0);
+                    for (int k = 0; k < C::BK / 16; k++) {
+                        const uint64_t ad = tc::sw128_desc(a0 + k * 2048, 8192, 1024);
+                        const uint64_t bd = tc::sw128_desc(b0 + k * 2048, 8192, 1024);
+                        tc::mma_f16(tmem, ad, bd, idesc, (g | c | k) != 0);
+                    }
                 }
                 tc::mma_commit(&empty[s]);
             }
@@ -323,11 +357,11 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <int BN, int STAGES, bool XA, bool IM2C>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1>
 cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUtensorMap &xmap, dim3 grid,
                       cudaStream_t st) {
-    using C = WgCfg<BN, STAGES, XA>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C>;
+    using C = WgCfg<BN, STAGES, XA, KB>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -338,21 +372,39 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     return cudaGetLastError();
 }
 
+// im2col path: two 64-pixel chunks per stage (64-wide tiles: 2 stages of 48 KB, two CTAs
+// per SM; 128 / 256-wide: 3 x 64 KB / 2 x 96 KB); cp.async path: one chunk per stage.
 template <bool IM2C>
 cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                           dim3 grid, cudaStream_t st) {
-    if (xa) {
+    if constexpr (IM2C) {
+        if (xa) {
+            switch (bn) {
+                case 64: return launch_wg<64, 2, true, IM2C, 2>(p, dymap, xmap, grid, st);
+                case 128: return launch_wg<128, 3, true, IM2C, 2>(p, dymap, xmap, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
         switch (bn) {
-            case 64: return launch_wg<64, 4, true, IM2C>(p, dymap, xmap, grid, st);
-            case 128: return launch_wg<128, 3, true, IM2C>(p, dymap, xmap, grid, st);
+            case 64: return launch_wg<64, 2, false, IM2C, 2>(p, dymap, xmap, grid, st);
+            case 128: return launch_wg<128, 3, false, IM2C, 2>(p, dymap, xmap, grid, st);
+            case 256: return launch_wg<256, 2, false, IM2C, 2>(p, dymap, xmap, grid, st);
             default: return cudaErrorInvalidValue;
         }
-    }
-    switch (bn) {
-        case 64: return launch_wg<64, 4, false, IM2C>(p, dymap, xmap, grid, st);
-        case 128: return launch_wg<128, 3, false, IM2C>(p, dymap, xmap, grid, st);
-        case 256: return launch_wg<256, 4, false, IM2C>(p, dymap, xmap, grid, st);
-        default: return cudaErrorInvalidValue;
+    } else {
+        if (xa) {
+            switch (bn) {
+                case 64: return launch_wg<64, 4, true, IM2C>(p, dymap, xmap, grid, st);
+                case 128: return launch_wg<128, 3, true, IM2C>(p, dymap, xmap, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        switch (bn) {
+            case 64: return launch_wg<64, 4, false, IM2C>(p, dymap, xmap, grid, st);
+            case 128: return launch_wg<128, 3, false, IM2C>(p, dymap, xmap, grid, st);
+            case 256: return launch_wg<256, 4, false, IM2C>(p, dymap, xmap, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
     }
 }
 

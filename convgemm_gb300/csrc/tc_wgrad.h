@@ -14,6 +14,10 @@ struct TcWgradParams {
     FastDiv dcp, dwo, dho;
     int *err;
     int im2col;               // X by im2col-mode TMA (Cp % 64 == 0), else by cp.async gathers
+    // one split: the epilogue writes dW itself (no workspace, no reduction) in the
+    // reference layout `layout` (0: [ci][kh][kw][co], 1: [co][ci][kh][kw]) of C channels
+    float *dw;
+    int direct, layout, C;
 };
 
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
