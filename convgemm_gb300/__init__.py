@@ -116,6 +116,10 @@ def lib():
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_launch_count.restype = ctypes.c_ulonglong
+        L.convgemm_dgrad_bf16_relu.argtypes = [SP, _VP, _VP, _VP, _VP, _VP]
+        L.convgemm_bias_grad_bf16_workspace_size.argtypes = [SP]
+        L.convgemm_bias_grad_bf16_workspace_size.restype = ctypes.c_size_t
+        L.convgemm_bias_grad_bf16.argtypes = [SP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
         _HG = [_I] * 14
         L.im2row_nhwc.argtypes = [_VP, _I, _VP] + _HG
         L.im2col_nchw.argtypes = [_VP, _I, _VP] + _HG

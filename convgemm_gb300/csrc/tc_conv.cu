@@ -386,6 +386,32 @@ __global__ void __launch_bounds__(288, 1)
                 } else {
                     tc::epi_bf16_64<false>(v0, v1, scp + c0, shp + c0, pk);
                 }
+                if (!C::OUTF32 && p.mask && m < M && nb < p.Cout) {
+                    // ReLU backward: keep the outputs where the mask (the activation the ReLU
+                    // produced, laid out like the output) is positive
+                    size_t pix = (size_t) m;
+                    if (!p.epi_tma) {
+                        uint32_t q, jw, j, b;
+                        cl.dwg.divmod(m, q, jw);
+                        cl.dhg.divmod(q, b, j);
+                        pix = ((size_t) b * p.Hout + cl.oy0 + cl.osy * (int) j) * p.Wout + cl.ox0 + cl.osx * (int) jw;
+                    }
+                    const __nv_bfloat16 *mrow = p.mask + pix * p.Cout + nb;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        uint4 mv = make_uint4(0, 0, 0, 0);
+                        if (nb + 8 * q + 8 <= p.Cout) mv = __ldg(reinterpret_cast<const uint4 *>(mrow) + q);
+                        const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const uint32_t lo = mw[e] & 0xFFFFu, hi = mw[e] >> 16;
+                            // positive: sign clear, not zero, not NaN
+                            const uint32_t klo = (lo - 1u) < 0x7F80u ? 0x0000FFFFu : 0u;
+                            const uint32_t khi = (hi - 1u) < 0x7F80u ? 0xFFFF0000u : 0u;
+                            pk[4 * q + e] &= klo | khi;
+                        }
+                    }
+                }
                 if (p.epi_tma) {
                     // each warp stages its 32 rows (4 KB) and stores them with its own TMA
                     // store: no barrier across the epilogue warps (out-of-range rows/columns

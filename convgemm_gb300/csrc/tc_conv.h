@@ -34,6 +34,7 @@ struct TcConvParams {
     const float *scale;        // per output channel, or NULL
     const float *shift;        // per output channel, or NULL
     int relu;
+    const __nv_bfloat16 *mask;   // BF16 tensor laid out like out, or NULL: out = 0 where mask <= 0 (ReLU backward)
     int B, Hin, Win, Cin, Hout, Wout, Cout;
     FastDiv dcin;
     int *err;                  // device error word for timed-out waits

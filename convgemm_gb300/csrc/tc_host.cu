@@ -277,7 +277,8 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
-                         const void *in_lo, const void *w_lo, int bn_override, int mt_override) {
+                         const void *in_lo, const void *w_lo, int bn_override, int mt_override,
+                         const void *mask) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
     TcConvParams p;
@@ -307,6 +308,7 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     p.scale = scale;
     p.shift = shift;
     p.relu = relu;
+    p.mask = (const __nv_bfloat16 *) mask;
     p.B = s.b;
     p.Hin = pl.Hin;
     p.Win = pl.Win;
@@ -451,8 +453,10 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
                   t.splits);
 }
 
-extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
-                                                 void *dx, void *stream) {
+namespace {
+
+convgemm_status_t dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
+                             const void *mask, void *stream) {
     if (convgemm_status_t e = check_tc_shape(shape, "convgemm_dgrad_bf16")) return e;
     if (!dy || !wpacked || !dx) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16: NULL tensor");
     if (shape->c % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "convgemm_dgrad_bf16: c must be a multiple of 8");
@@ -469,7 +473,21 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, 
     }
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
-    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits);
+    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits, mask);
+}
+
+}  // namespace
+
+extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
+                                                 void *dx, void *stream) {
+    return dgrad_bf16(shape, dy, wpacked, dx, nullptr, stream);
+}
+
+extern "C" convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *shape, const void *dy,
+                                                      const void *wpacked, void *dx, const void *x, void *stream) {
+    if (!x || ((uintptr_t) x & 15))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16_relu: x NULL or not 16-byte aligned");
+    return dgrad_bf16(shape, dy, wpacked, dx, x, stream);
 }
 
 // ------------------------------------------------------- weight gradient
@@ -721,3 +739,26 @@ extern "C" convgemm_status_t convgemm_prep_launch(const void *table, int njobs, 
     return cg_cuda_check(prep_group_launch((const PrepJob *) table, njobs, nblocks, (cudaStream_t) stream),
                          "grouped preparation launch");
 }
+
+// ------------------------------------------------------------ bias gradient
+extern "C" size_t convgemm_bias_grad_bf16_workspace_size(const convgemm_shape_t *shape) {
+    if (check_tc_shape(shape, "convgemm_bias_grad_bf16_workspace_size")) return 0;
+    const ConvGeom g = make_geom(cg_from_public(*shape));
+    return sizeof(float) * (size_t) tc_bias_grad_groups(g.P) * shape->kn;
+}
+
+extern "C" convgemm_status_t convgemm_bias_grad_bf16(const convgemm_shape_t *shape, const void *dy, float *db,
+                                                     void *workspace, size_t workspace_bytes, void *stream) {
+    const char *fn = "convgemm_bias_grad_bf16";
+    if (convgemm_status_t e = check_tc_shape(shape, fn)) return e;
+    if (!dy || !db || !workspace) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL argument", fn);
+    const size_t need = convgemm_bias_grad_bf16_workspace_size(shape);
+    if (workspace_bytes < need)
+        return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "%s: workspace %zu bytes < %zu needed", fn, workspace_bytes, need);
+    const ConvGeom g = make_geom(cg_from_public(*shape));
+    if (g.P > (1LL << 31) - 1) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: too many pixels", fn);
+    return cg_cuda_check(tc_bias_grad(dy, g.P, shape->kn, round_up(shape->kn, 8), db, (float *) workspace,
+                                      (cudaStream_t) stream),
+                         fn);
+}
+

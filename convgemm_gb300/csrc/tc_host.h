@@ -40,4 +40,4 @@ bool tc_tune_get(int op, const convgemm_shape_t &s, TcTune *t);
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,
                          const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0,
-                         int mt_override = 0);
+                         int mt_override = 0, const void *mask = nullptr);

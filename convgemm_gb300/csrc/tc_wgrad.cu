@@ -443,3 +443,50 @@ cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, in
     wgrad_reduce_kernel<<<grid, block, 0, st>>>(src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout); cg_note_launch();
     return cudaGetLastError();
 }
+
+// ------------------------------------------------------------ bias gradient
+// db[co] = sum over the P pixels of dY[p][co] (dY BF16 [P][ld]), FP32, in a fixed
+// order: pass 1 sums `rows` consecutive pixels per (group, 64-channel chunk) with
+// four interleaved row streams combined in order; pass 2 adds the groups in order.
+namespace {
+
+__global__ void __launch_bounds__(256) bias_grad_pass1(const __nv_bfloat16 *__restrict__ dy, int P, int kn, int ld,
+                                                       int rows, float *__restrict__ part) {
+    __shared__ float acc[4][64];
+    const int ch = blockIdx.x * 64 + (threadIdx.x & 63), r0 = threadIdx.x >> 6;
+    const int p0 = blockIdx.y * rows, p1 = min(P, p0 + rows);
+    float sacc = 0.0f;
+    if (ch < kn)
+        for (int p = p0 + r0; p < p1; p += 4) sacc = __fadd_rn(sacc, __bfloat162float(dy[(size_t) p * ld + ch]));
+    acc[r0][threadIdx.x & 63] = sacc;
+    __syncthreads();
+    if (r0 == 0 && ch < kn)
+        part[(size_t) blockIdx.y * kn + ch] =
+            __fadd_rn(__fadd_rn(__fadd_rn(acc[0][threadIdx.x], acc[1][threadIdx.x]), acc[2][threadIdx.x]),
+                      acc[3][threadIdx.x]);
+}
+
+__global__ void bias_grad_pass2(const float *__restrict__ part, int groups, int kn, float *__restrict__ db) {
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= kn) return;
+    float sacc = 0.0f;
+    for (int g = 0; g < groups; g++) sacc = __fadd_rn(sacc, part[(size_t) g * kn + ch]);
+    db[ch] = sacc;
+}
+
+}  // namespace
+
+int tc_bias_grad_groups(long long P) {
+    long long g = (P + 1023) / 1024;   // about 1024 pixels per group
+    return (int) (g > 256 ? 256 : (g < 1 ? 1 : g));
+}
+
+cudaError_t tc_bias_grad(const void *dy, long long P, int kn, int ld, float *db, float *part, cudaStream_t st) {
+    const int groups = tc_bias_grad_groups(P);
+    const int rows = (int) ((P + groups - 1) / groups);
+    dim3 g1((kn + 63) / 64, groups);
+    bias_grad_pass1<<<g1, 256, 0, st>>>((const __nv_bfloat16 *) dy, (int) P, kn, ld, rows, part); cg_note_launch();
+    bias_grad_pass2<<<(kn + 127) / 128, 128, 0, st>>>(part, groups, kn, db); cg_note_launch();
+    return cudaGetLastError();
+}
+

@@ -30,3 +30,8 @@ int tc_wgrad_groups(int splits);
 // ws: [splits + tc_wgrad_groups(splits)][Nx * kn] FP32.
 cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, int kn, int C, int Cp, int kh, int kw,
                             int layout, cudaStream_t st);
+
+// Bias gradient db[co] = sum_p dY[p][co] (BF16 dY [P][ld]), deterministic;
+// part: tc_bias_grad_groups(P) * kn FP32 scratch.
+int tc_bias_grad_groups(long long P);
+cudaError_t tc_bias_grad(const void *dy, long long P, int kn, int ld, float *db, float *part, cudaStream_t st);

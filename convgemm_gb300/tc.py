@@ -44,6 +44,22 @@ def dgrad_bf16(shape: Shape, dy, wpacked, dx, stream=None):
     _raise_if(lib().convgemm_dgrad_bf16(ctypes.byref(shape), ptr(dy), ptr(wpacked), ptr(dx), _stream(stream)))
 
 
+def dgrad_bf16_relu(shape: Shape, dy, wpacked, dx, x, stream=None):
+    """Input gradient times the derivative of the ReLU that produced x (dx = 0 where x <= 0)."""
+    _raise_if(lib().convgemm_dgrad_bf16_relu(ctypes.byref(shape), ptr(dy), ptr(wpacked), ptr(dx), ptr(x),
+                                             _stream(stream)))
+
+
+def bias_grad_bf16(shape: Shape, dy, db, workspace=None, stream=None):
+    """db[co] = sum over output pixels of dy[p][co] (FP32, fixed order)."""
+    import torch
+    n = lib().convgemm_bias_grad_bf16_workspace_size(ctypes.byref(shape))
+    if workspace is None:
+        workspace = torch.empty(n // 4 + 1, device=dy.device)
+    _raise_if(lib().convgemm_bias_grad_bf16(ctypes.byref(shape), ptr(dy), ptr(db), ptr(workspace),
+                                            workspace.numel() * workspace.element_size(), _stream(stream)))
+
+
 def wgrad_bf16_workspace_size(shape: Shape) -> int:
     return lib().convgemm_wgrad_bf16_workspace_size(ctypes.byref(shape))
 

@@ -252,6 +252,19 @@ convgemm_status_t convgemm_group_launch(const void *table, int n, int total_tile
  * count (the number of 64-pixel chunks).  Any pointer may be NULL. */
 convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *shape, int *bn, int *splits, int *max_splits);
 
+/* Input gradient followed by the backward of the ReLU that produced the layer's
+ * input x: dx = dgrad(dy, w) where x > 0, else 0 (x: the BF16 NHWC input of the
+ * forward pass, [b][h][w][c]).  The masking is fused into the kernel's epilogue. */
+convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
+                                           const void *x, void *stream);
+
+/* Bias gradient of the convolution: db[co] = sum over the b*ho*wo output pixels of
+ * dy[p][co] (dy BF16 NHWC with kn rounded up to 8 channels, as for
+ * convgemm_wgrad_bf16), FP32 in a fixed order (bit-reproducible). */
+size_t convgemm_bias_grad_bf16_workspace_size(const convgemm_shape_t *shape);
+convgemm_status_t convgemm_bias_grad_bf16(const convgemm_shape_t *shape, const void *dy, float *db, void *workspace,
+                                          size_t workspace_bytes, void *stream);
+
 /* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
 size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);
 

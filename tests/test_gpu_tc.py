@@ -307,3 +307,48 @@ def test_two_m_tiles_strided_input_gradient(cglib, oracle_lib):
         assert rel_max_rms(outs[1][0].float().cpu().numpy(), ref)[0] <= BF16_TOL
     finally:
         tc.tune_clear()
+
+
+@pytest.mark.parametrize("shape", [(2, 14, 14, 64, 128, 3, 1, 1, 1), (2, 9, 9, 128, 64, 3, 1, 2, 1),
+                                   (2, 8, 8, 256, 512, 1, 0, 2, 1)], ids=str)
+def test_dgrad_relu_mask_fused(cglib, shape):
+    """The ReLU-backward mask fused into the input-gradient epilogue equals the unmasked
+    input gradient with the entries where x <= 0 zeroed, bit for bit."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(c + kn)
+    wt = (rng.standard_normal(k * k * c * kn) * 0.1).astype(np.float32)
+    x = torch.from_numpy(rng.standard_normal(b * h * w * c).astype(np.float32)).cuda().to(torch.bfloat16)
+    x = torch.relu(x) - (torch.rand(x.shape, device="cuda") < 0.1).to(torch.bfloat16)   # zeros, and some negatives
+    dy = to_dev_bf16_nhwc(cg, tc, rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32), b, kn, s.ho, s.wo)
+    wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
+    tc.dgrad_bf16(s, dy, wpd, dx)
+    dxm = torch.full_like(dx, float("nan"))
+    tc.dgrad_bf16_relu(s, dy, wpd, dxm, x.reshape(b, h, w, c).contiguous())
+    torch.cuda.synchronize()
+    cg.check_device()
+    want = torch.where(x.reshape(b, h, w, c) > 0, dx, torch.zeros_like(dx))
+    assert torch.equal(dxm.view(torch.int16), want.view(torch.int16))
+
+
+@pytest.mark.parametrize("shape", [(2, 14, 14, 64, 96, 3, 1, 1, 1), (8, 28, 28, 64, 256, 1, 0, 1, 1)], ids=str)
+def test_bias_grad_against_fp64(cglib, shape):
+    """db = sum over output pixels of dY: within FP32 rounding of FP64, and reproducible."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(kn)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    db1, db2 = torch.empty(kn, device="cuda"), torch.empty(kn, device="cuda")
+    tc.bias_grad_bf16(s, dyd, db1)
+    tc.bias_grad_bf16(s, dyd, db2)
+    torch.cuda.synchronize()
+    cg.check_device()
+    assert torch.equal(db1, db2)
+    ref = bf16r(dy).astype(np.float64).reshape(-1, kn).sum(0)
+    assert np.abs(db1.cpu().numpy() - ref).max() <= 1e-5 * np.abs(bf16r(dy)).reshape(-1, kn).sum(0).max()
