@@ -491,6 +491,29 @@ class VggNet:
             self.L.append(d)
         self.ws32 = torch.empty(ws32 // 4 + 1, device="cuda")
         self.ws16 = torch.empty(ws16 // 4 + 1, device="cuda")
+        self.side = torch.cuda.Stream()
+        self.prep = tc.Prep([dict(layout=cg.NCHW, shape=d["s"], weights=d["w32"], packed_fwd=d["wp"],
+                                  packed_dgrad=d["wpd"], bias=d["bias"], scale=d["scale"], shift=d["shift"])
+                             for d in self.L])
+
+    def tune_items(self):
+        tc, cg = self.tc, self.cg
+        items = []
+        for d in self.L:
+            s = d["s"]
+            items.append({"op": tc.TUNE_FWD, "shape": s, "run": lambda ws, d=d, s=s: tc.fwd_bf16(
+                s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=True)})
+            if not d["first"]:
+                items.append({"op": tc.TUNE_DGRAD, "shape": s,
+                              "run": lambda ws, d=d, s=s: tc.dgrad_bf16(s, d["dyb"], d["wpd"], d["dxb"])})
+            items.append({"op": tc.TUNE_WGRAD, "shape": s, "run": lambda ws, d=d, s=s: tc.wgrad_bf16(
+                cg.NCHW, s, d["dyb"], d["xb"], d["dwb"], ws)})
+        return items
+
+    def resize_workspace(self):
+        need = max(self.tc.wgrad_bf16_workspace_size(d["s"]) for d in self.L)
+        if need > self.ws16.numel() * 4:
+            self.ws16 = self.torch.empty(need // 4 + 1, device="cuda")
 
     def step_f32(self):
         cg = self.cg
@@ -506,18 +529,27 @@ class VggNet:
             self.cg.wgrad_f32(self.cg.NCHW, d["s"], d["dy32"], d["x32"], d["dw32"], self.ws32)
 
     def step_bf16(self):
-        cg, tc = self.cg, self.tc
+        """The BF16 form of the step: one grouped preparation (bias folds, OIHW weight packings),
+        then per layer the NCHW FP32 -> NHWC BF16 conversions and the convolutions, scheduled on
+        two streams: the forward chain, then the input-gradient chain on the main stream with each
+        layer's weight gradient on the second stream as soon as its dY has been converted."""
+        torch, cg, tc = self.torch, self.cg, self.tc
+        main, side = torch.cuda.current_stream(), self.side
+        self.prep.launch(main)
         for d in self.L:
             s = d["s"]
-            tc.to_bf16_nhwc(cg.NCHW, s.b, s.c, s.h, s.w, d["x32"], d["xb"])
-            tc.to_bf16_nhwc(cg.NCHW, s.b, s.kn, s.h, s.w, d["dy32"], d["dyb"])
-            tc.fold_epilogue(s.kn, d["scale"], d["shift"], bias=d["bias"])
-            tc.pack_weights(cg.NCHW, s, tc.OPERAND_FWD, d["w32"], d["wp"])
-            tc.fwd_bf16(s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=True)
+            tc.to_bf16_nhwc(cg.NCHW, s.b, s.c, s.h, s.w, d["x32"], d["xb"], stream=main)
+            tc.fwd_bf16(s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=True, stream=main)
+        for d in reversed(self.L):
+            s = d["s"]
+            tc.to_bf16_nhwc(cg.NCHW, s.b, s.kn, s.h, s.w, d["dy32"], d["dyb"], stream=main)
+            ev = torch.cuda.Event()
+            ev.record(main)
+            side.wait_event(ev)
+            tc.wgrad_bf16(cg.NCHW, s, d["dyb"], d["xb"], d["dwb"], self.ws16, stream=side)
             if not d["first"]:
-                tc.pack_weights(cg.NCHW, s, tc.OPERAND_DGRAD, d["w32"], d["wpd"])
-                tc.dgrad_bf16(s, d["dyb"], d["wpd"], d["dxb"])
-            tc.wgrad_bf16(cg.NCHW, s, d["dyb"], d["xb"], d["dwb"], self.ws16)
+                tc.dgrad_bf16(s, d["dyb"], d["wpd"], d["dxb"], stream=main)
+        main.wait_stream(side)
 
     def wgrad_bf16(self):
         for d in self.L:
@@ -614,6 +646,12 @@ def run_vgg(args):
     net = VggNet(torch, cg, tc, layers, batch)
     flops = sum(conv_flops(l, batch) * (2 if i == 0 else 3) for i, l in enumerate(layers))
     net.step_bf16()
+    torch.cuda.synchronize()
+    from convgemm_gb300 import autotune
+    t0 = time.perf_counter()
+    tune_stats = None if args.no_autotune else autotune.tune_ops(net.tune_items())
+    tune_s = time.perf_counter() - t0
+    net.resize_workspace()
     net.step_f32()
     torch.cuda.synchronize()
     cg.check_device()
@@ -692,10 +730,11 @@ def run_vgg(args):
                 "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
                 "config": {"workload": "vgg16: 13 3x3/s1/p1 convs at 224x224, fwd (bias + ReLU) + dX (not layer 1) "
                                        "+ dW, NCHW FP32 tensors; the BF16 form converts x and dY to NHWC BF16 and "
-                                       "packs OIHW weights inside the step, dW in OIHW FP32",
+                                       "packs OIHW weights inside the step (one grouped launch), dW in OIHW FP32",
+                           "schedule": "two streams: forward chain; dgrad chain with each wgrad beside it",
                            "global_batch": batch * world, "per_gpu_batch": batch, "seq_len": None,
                            "parallelism": f"replicas{world}", "l2": "inputs larger than L2",
-                           "gflop_per_img": flops / batch / 1e9},
+                           "gflop_per_img": flops / batch / 1e9, "autotune": tune_stats, "autotune_s": tune_s},
                 "tflops": tf,
                 "fp32_plain": {"value": world * batch / (ms32 / 1000), "unit": "img/s", "ms_per_step": ms32,
                                "tflops": flops / (ms32 / 1000) / 1e12},
@@ -780,6 +819,20 @@ def run_forms(args):
         L.append(d)
     torch.cuda.synchronize()
     cg.check_device()
+    from convgemm_gb300 import autotune
+    items = []
+    for d in L:
+        s = d["s"]
+        items.append({"op": tc.TUNE_FWD, "shape": s, "run": lambda ws, d=d, s=s: tc.fwd_bf16(
+            s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=d["relu"])})
+        if d["fp8"]:
+            items.append({"op": tc.TUNE_FWD_FP8, "shape": s, "run": lambda ws, d=d, s=s: tc.fwd_fp8(
+                s, d["xq"], d["wq"], d["y8"], d["sc8"], d["sh8"], relu=d["relu"])})
+            items.append({"op": tc.TUNE_FWD_BF16X3, "shape": s, "run": lambda ws, d=d, s=s: tc.fwd_bf16x3(
+                s, d["xh"], d["xl"], d["wh"], d["wl"], d["y3"], d["scale"], d["shift"], relu=d["relu"])})
+    t0 = time.perf_counter()
+    tune_stats = None if args.no_autotune else autotune.tune_ops(items)
+    tune_s = time.perf_counter() - t0
 
     def fwd(form):
         def run():
@@ -864,7 +917,7 @@ def run_forms(args):
                                        "3xBF16 on the 52 layers with channels a multiple of 64 (the stem stays BF16 "
                                        "and is not counted in their lines)",
                            "global_batch": batch * world, "parallelism": f"replicas{world}",
-                           "l2": "inputs larger than L2"},
+                           "l2": "inputs larger than L2", "autotune": tune_stats, "autotune_s": tune_s},
                 "forms": res,
                 "roofline": {"bound": "tensor", "kernel": "tc_conv_kernel (FP8 forward)",
                              "achieved": res["fp8"]["tflops"], "peak": peaks["bf16_tflops"] * 2,
