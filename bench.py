@@ -93,6 +93,15 @@ class ClockSampler:
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+        # start timing only once the sampler is producing samples
+        t0 = time.time()
+        while self.p is not None and time.time() - t0 < 3.0:
+            try:
+                if os.path.getsize(self.f.name) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.02)
 
     def stop(self):
         if self.p is None:
@@ -1064,7 +1073,7 @@ def run_grouped(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
