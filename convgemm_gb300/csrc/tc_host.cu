@@ -58,6 +58,23 @@ EncodeIm2colFn encode_im2col_fn() {
 
 // im2col-mode map of a BF16 NHWC tensor [B][H][W][C]: `pixels` pixels x 64 channels per load,
 // bounding box [lo, dim-1+up] per spatial dimension, traversal strides (sh, sw), 128-byte swizzle.
+convgemm_status_t tc_make_map_4d_box(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int box_h,
+                                     int box_w) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    if (((uintptr_t) ptr & 15) || (C * 2) % 16)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA operand not 16-byte aligned");
+    cuuint64_t dims[4] = {(cuuint64_t) C, (cuuint64_t) W, (cuuint64_t) H, (cuuint64_t) B};
+    cuuint64_t strides[3] = {(cuuint64_t) C * 2, (cuuint64_t) W * C * 2, (cuuint64_t) H * W * C * 2};
+    cuuint32_t box[4] = {(cuuint32_t) C, (cuuint32_t) box_w, (cuuint32_t) box_h, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int) r);
+    return CONVGEMM_SUCCESS;
+}
+
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes) {
     EncodeIm2colFn fn = encode_im2col_fn();
@@ -447,6 +464,8 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     tc_plan_fwd(s, pl);
+    if (tc_stem_applicable(s))   // c <= 8, output rows of <= 128 pixels: input slabs staged in shared memory
+        return tc_stem_run(s, x, wpacked, pl.Ktot, y, scale, shift, relu, (cudaStream_t) stream);
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_FWD, *shape, &t);
     return tc_run(pl, s, x, wpacked, y, scale, shift, relu, (cudaStream_t) stream, 0, nullptr, nullptr, t.bn,

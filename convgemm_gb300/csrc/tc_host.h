@@ -25,7 +25,14 @@ convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, in
                                     long long rows, long long cols, int box_cols, int box_rows, CUtensorMapSwizzle sw);
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
+// 4-D NHWC BF16 map [B][H][W][C] with a {C, box_w, box_h, 1} box, no swizzle.
+convgemm_status_t tc_make_map_4d_box(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int box_h,
+                                     int box_w);
 bool tc_plan_im2col(TcPlan &pl);
+// Forward of convolutions with at most 8 input channels (tc_stem.cu).
+bool tc_stem_applicable(const cg_shape &s);
+convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,
+                              const float *scale, const float *shift, int relu, cudaStream_t st);
 
 int tc_num_sms();
 // Autotuned tile configuration of one operation on one shape (0 = heuristic):
