@@ -117,6 +117,7 @@ def lib():
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_launch_count.restype = ctypes.c_ulonglong
         L.convgemm_dgrad_bf16_relu.argtypes = [SP, _VP, _VP, _VP, _VP, _VP]
+        L.convgemm_selftest_wait_timeout.argtypes = [ctypes.c_uint, _VP]
         L.convgemm_bias_grad_bf16_workspace_size.argtypes = [SP]
         L.convgemm_bias_grad_bf16_workspace_size.restype = ctypes.c_size_t
         L.convgemm_bias_grad_bf16.argtypes = [SP, _VP, _VP, _VP, ctypes.c_size_t, _VP]

@@ -55,7 +55,8 @@ constexpr uint64_t WAIT_BUDGET_NS = 2000000000ull;  // 2 s
 // loop just polls it (a software sleep would wake late and stall the ring);
 // the clock is read every 1024 polls.  On timeout it records `code` in *err
 // (first writer wins) and returns false; callers then stop waiting.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+__device__ __forceinline__ bool mbar_wait_budget(uint64_t *bar, uint32_t parity, int *err, int code,
+                                                 uint64_t budget_ns) {
     uint64_t t0 = 0;
     for (uint32_t i = 1;; i++) {
         if (mbar_try_wait(bar, parity)) return true;
@@ -63,12 +64,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *e
             const uint64_t now = globaltimer();
             if (t0 == 0) {
                 t0 = now;
-            } else if (now - t0 > WAIT_BUDGET_NS) {
+            } else if (now - t0 > budget_ns) {
                 if (err) atomicCAS(err, 0, code);
                 return false;
             }
         }
     }
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+    return mbar_wait_budget(bar, parity, err, code, WAIT_BUDGET_NS);
 }
 
 // ------------------------------------------------------------- cp.async

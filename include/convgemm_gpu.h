@@ -58,6 +58,13 @@ typedef struct {
 /* Status and message of the last failing call on this host thread. */
 convgemm_status_t convgemm_get_last_status(void);
 
+/* Self-test of the failure path: launches a kernel whose device-side wait runs
+ * out after budget_ms (1..1000) because nothing completes its barrier; the kernel
+ * records CONVGEMM_SELFTEST_WAIT_CODE in the device error word and returns, and
+ * the next convgemm_check_device returns CONVGEMM_ERROR_TIMEOUT (and clears it). */
+#define CONVGEMM_SELFTEST_WAIT_CODE 99
+convgemm_status_t convgemm_selftest_wait_timeout(unsigned budget_ms, void *stream);
+
 /* Number of GPU kernels the library has launched (or recorded into a stream
  * capture) in this process: a diagnostic for counting launches per step. */
 unsigned long long convgemm_launch_count(void);
