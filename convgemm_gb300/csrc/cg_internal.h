@@ -49,3 +49,25 @@ cudaError_t cg_helper_col2im(const float *cols, float *out, int b, int c, int h,
                              int vpad, int hpad, int vstr, int hstr, int vdil, int hdil, cudaStream_t st);
 cudaError_t cg_helper_transpose(int rows, int cols, const float *in, int ld, float beta, float *out, int kn, int ho,
                                 int wo, int start_row, int start_col, cudaStream_t st);
+
+// Launch with programmatic stream serialization (the kernel must call
+// tc::pdl_wait() before its first global memory access); plain launch when the
+// environment sets CONVGEMM_NO_PDL=1.  Counts the launch.
+bool cg_pdl_enabled();
+template <typename... KArgs, typename... Args>
+cudaError_t cg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                          Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = cg_pdl_enabled() ? 1 : 0;
+    cg_note_launch();
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...);
+}
+

@@ -2,6 +2,7 @@
 // argument checks, error reporting, host-pointer staging and the cached
 // device buffers the void drop-in entry points need.
 #include <atomic>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,14 @@ convgemm_status_t cg_cuda_check(cudaError_t e, const char *what) {
     if (e == cudaSuccess) return CONVGEMM_SUCCESS;
     return cg_set_error(e == cudaErrorMemoryAllocation ? CONVGEMM_ERROR_ALLOC : CONVGEMM_ERROR_CUDA,
                         "%s: %s", what, cudaGetErrorString(e));
+}
+
+bool cg_pdl_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("CONVGEMM_NO_PDL");
+        return !(e && e[0] == '1');
+    }();
+    return on;
 }
 
 static std::atomic<unsigned long long> g_launches{0};

@@ -6,6 +6,7 @@
 
 #include "cg_common.cuh"
 #include "prep.h"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -211,6 +212,8 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const PrepJob *__restri
                                                          int njobs) {
     __shared__ float tile[32][33];
     extern __shared__ int s_b0[];
+    tc::pdl_wait();
+    tc::pdl_trigger();
     for (int i = threadIdx.x; i < njobs; i += blockDim.x) s_b0[i] = __ldg(b0 + i);
     __syncthreads();
     int lo = 0, hi = njobs - 1;
@@ -374,6 +377,5 @@ cudaError_t prep_pack_split(const float *w, int nchw, int C, int kh, int kw, int
 
 cudaError_t prep_group_launch(const PrepJob *jobs, int njobs, int nblocks, cudaStream_t st) {
     const int *b0 = (const int *) (jobs + njobs);
-    prep_group_kernel<<<nblocks, 256, sizeof(int) * njobs, st>>>(jobs, b0, njobs); cg_note_launch();
-    return cudaGetLastError();
+    return cg_launch_pdl(prep_group_kernel, dim3(nblocks), dim3(256), sizeof(int) * njobs, st, jobs, b0, njobs);
 }

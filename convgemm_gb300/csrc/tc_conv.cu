@@ -186,6 +186,9 @@ __global__ void __launch_bounds__(288, 1)
         d.ktiles = c.ktiles; d.tile0 = c.tile0; d.lo_y = c.lo_y; d.lo_x = c.lo_x; d.mint_y = c.mint_y;
         d.mint_x = c.mint_x; d.dwg = c.dwg; d.dhg = c.dhg;
     }
+    // everything above touched only shared memory and kernel parameters
+    tc::pdl_wait();
+    tc::pdl_trigger();
     if (sc_all)
         for (int n = threadIdx.x; n < p.Cout; n += blockDim.x) {
             sc_tab[n] = p.scale ? __ldg(p.scale + n) : 1.0f;
@@ -535,8 +538,7 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUte
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, C::THREADS, C::SMEM, st>>>(p, wmap, omap, amaps); cg_note_launch();
-    return cudaGetLastError();
+    return cg_launch_pdl(kern, dim3(grid), dim3(C::THREADS), C::SMEM, st, p, wmap, omap, amaps);
 }
 
 }  // namespace

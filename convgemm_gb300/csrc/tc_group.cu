@@ -73,6 +73,8 @@ __global__ void __launch_bounds__(288, 1)
     float *sh_tab = sc_tab + GBN;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    tc::pdl_wait();
+    tc::pdl_trigger();
     // a table prepared for another count, or a tile count beyond the table: run nothing
     if (__ldg(&probs[0].count) != nprob) {
         if (threadIdx.x == 0) atomicCAS(err, 0, 25);
@@ -364,6 +366,7 @@ extern "C" convgemm_status_t convgemm_group_launch(const void *table, int n, int
     }
     const int sms = tc_num_sms();
     const int grid = total_tiles < sms ? total_tiles : sms;
-    tc_group_kernel<<<grid, 288, GSMEM, (cudaStream_t) stream>>>((const GroupProblem *) table, n, total_tiles, err); cg_note_launch();
-    return cg_cuda_check(cudaGetLastError(), "grouped kernel launch");
+    return cg_cuda_check(cg_launch_pdl(tc_group_kernel, dim3(grid), dim3(288), GSMEM, (cudaStream_t) stream,
+                                       (const GroupProblem *) table, n, total_tiles, err),
+                         "grouped kernel launch");
 }

@@ -20,6 +20,15 @@ __device__ __forceinline__ uint64_t globaltimer() {
     return t;
 }
 
+// ------------------------------------------------ programmatic dependent launch
+// A kernel launched with programmatic stream serialization may start while the
+// previous kernel of its stream is still running: pdl_wait() blocks until that
+// kernel has completed and its memory is visible, so no global memory may be read
+// or written before it; pdl_trigger() then lets the next kernel start launching.
+// Both are no-ops for kernels launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ------------------------------------------------------------- mbarrier
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");

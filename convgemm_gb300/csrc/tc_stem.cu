@@ -66,6 +66,8 @@ __global__ void __launch_bounds__(288, 1)
     tc_stem_kernel(const __grid_constant__ StemParams p, const __grid_constant__ CUtensorMap xmap,
                    const __grid_constant__ CUtensorMap wmap) {
     using C = StemCfg<BN>;
+    tc::pdl_wait();   // the weights are loaded in the prologue
+    tc::pdl_trigger();
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *wres = base + STEM_STAGES * C::STAGE;   // resident weights: K block j at j * B_BYTES
@@ -267,8 +269,7 @@ cudaError_t launch_stem(const StemParams &p, const CUtensorMap &x, const CUtenso
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    tc_stem_kernel<BN><<<grid, 288, StemCfg<BN>::SMEM, st>>>(p, x, w); cg_note_launch();
-    return cudaGetLastError();
+    return cg_launch_pdl(tc_stem_kernel<BN>, dim3(grid), dim3(288), StemCfg<BN>::SMEM, st, p, x, w);
 }
 
 }  // namespace

@@ -70,6 +70,8 @@ __global__ void __launch_bounds__(160, 1)
         tc::tmem_alloc(tmem_holder, BN);
         tc::tmem_relinquish();
     }
+    tc::pdl_wait();   // no global memory access above
+    tc::pdl_trigger();
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
@@ -282,6 +284,8 @@ __global__ void __launch_bounds__(160, 1)
 // grouping depends only on the split count, so results stay bit-reproducible.
 __global__ void wgrad_group_sum_kernel(const float *__restrict__ ws, float *__restrict__ gs, int splits, int per,
                                        size_t plane) {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     const size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x;
     if (i >= plane) return;
     const int z0 = blockIdx.y * per, z1 = min(splits, z0 + per);
@@ -304,6 +308,8 @@ __global__ void wgrad_group_sum_kernel(const float *__restrict__ ws, float *__re
 // contiguous dimension, summed z = 0, 1, ... in order, and written through shared memory.
 __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restrict__ dw, int splits, int xa, int Nx,
                                     int kn, int C, int Cp, int khw, int layout) {
+    tc::pdl_wait();
+    tc::pdl_trigger();
     __shared__ float tile[32][33];
     const int co0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -368,8 +374,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    kern<<<grid, 160, C::SMEM, st>>>(p, map, xmap); cg_note_launch();
-    return cudaGetLastError();
+    return cg_launch_pdl(kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
 }
 
 // im2col path: two 64-pixel chunks per stage (64-wide tiles: 2 stages of 48 KB, two CTAs
@@ -435,13 +440,14 @@ cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, in
         float *gs = ws + (size_t) splits * plane;
         const int per = (splits + groups - 1) / groups;
         dim3 g1((unsigned) ((plane + 255) / 256), groups);
-        wgrad_group_sum_kernel<<<g1, 256, 0, st>>>(ws, gs, splits, per, plane); cg_note_launch();
+        if (cudaError_t e = cg_launch_pdl(wgrad_group_sum_kernel, g1, dim3(256), 0, st, (const float *) ws, gs, splits,
+                                          per, plane))
+            return e;
         src = gs;
         n = groups;
     }
     dim3 grid((kn + 31) / 32, (Nx + 31) / 32), block(32, 8);
-    wgrad_reduce_kernel<<<grid, block, 0, st>>>(src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout); cg_note_launch();
-    return cudaGetLastError();
+    return cg_launch_pdl(wgrad_reduce_kernel, grid, block, 0, st, src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout);
 }
 
 // ------------------------------------------------------------ bias gradient
