@@ -300,6 +300,9 @@ class Net:
                 main.wait_stream(side)
         ready = torch.cuda.Event()
         ready.record(main)
+        # the weight gradients fill the SMs the input-gradient chain leaves idle: no early
+        # (programmatic) launches on the chain while they run
+        pdl = cg.set_pdl(0)
         for d in reversed(self.L):
             s = d["s"]
             side.wait_event(ready)
@@ -308,6 +311,7 @@ class Net:
                 tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"], stream=main)
                 ready = torch.cuda.Event()
                 ready.record(main)
+        cg.set_pdl(pdl)
         main.wait_stream(side)
 
     def step_family(self, fam):
@@ -549,6 +553,7 @@ class VggNet:
             s = d["s"]
             tc.to_bf16_nhwc(cg.NCHW, s.b, s.c, s.h, s.w, d["x32"], d["xb"], stream=main)
             tc.fwd_bf16(s, d["xb"], d["wp"], d["yb"], d["scale"], d["shift"], relu=True, stream=main)
+        pdl = cg.set_pdl(0)   # no early launches on the chain while the weight gradients run beside it
         for d in reversed(self.L):
             s = d["s"]
             tc.to_bf16_nhwc(cg.NCHW, s.b, s.kn, s.h, s.w, d["dy32"], d["dyb"], stream=main)
@@ -558,6 +563,7 @@ class VggNet:
             tc.wgrad_bf16(cg.NCHW, s, d["dyb"], d["xb"], d["dwb"], self.ws16, stream=side)
             if not d["first"]:
                 tc.dgrad_bf16(s, d["dyb"], d["wpd"], d["dxb"], stream=main)
+        cg.set_pdl(pdl)
         main.wait_stream(side)
 
     def wgrad_bf16(self):

@@ -116,6 +116,8 @@ def lib():
         L.convgemm_bf16x3_pack_weights.argtypes = [_I, SP, _VP, _VP, _VP, _VP]
         L.convgemm_fwd_bf16x3.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_launch_count.restype = ctypes.c_ulonglong
+        L.convgemm_set_pdl.argtypes = [_I]
+        L.convgemm_set_pdl.restype = _I
         L.convgemm_dgrad_bf16_relu.argtypes = [SP, _VP, _VP, _VP, _VP, _VP]
         L.convgemm_selftest_wait_timeout.argtypes = [ctypes.c_uint, _VP]
         L.convgemm_bias_grad_bf16_workspace_size.argtypes = [SP]
@@ -190,6 +192,13 @@ def transpose_nchw(rows, cols, x, ld, beta, out, kn, ho, wo, start_row, start_co
 def launch_count() -> int:
     """Kernels launched (or captured) by the library so far in this process."""
     return int(lib().convgemm_launch_count())
+
+
+def set_pdl(on: int) -> int:
+    """Programmatic dependent launch of the persistent chain kernels for this host
+    thread: 1 on, 0 off, -1 default (on unless CONVGEMM_NO_PDL=1).  Returns the
+    previous setting.  Turn it off while other streams run work beside the chain."""
+    return int(lib().convgemm_set_pdl(int(on)))
 
 
 def last_error() -> tuple[int, str]:

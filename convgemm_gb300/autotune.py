@@ -29,7 +29,7 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
-OP_CACHE_TAG = "v3"   # op entries: fwd / dgrad with the M-tile choice, wgrad with 2-chunk stages and direct single-split writes
+OP_CACHE_TAG = "v4"   # op entries: fwd / dgrad with the M-tile choice; wgrad with 2-chunk stages, direct single-split writes and 2..8-split clusters
 
 
 def cache_path() -> str:
@@ -183,7 +183,8 @@ def op_candidates(op: int, s):
     tc.tune_set(op, s, 0, 0)
     bn0, s0, mx = tc.wgrad_bf16_plan(s)
     widths = [64, 128] if s.kn < 128 else candidate_widths(s.kh * s.kw * tc.c8(s.c))
-    splits = sorted({max(1, s0 // 4), max(1, s0 // 2), s0, min(mx, 2 * s0)})
+    # around the heuristic, plus the cluster-reduced split counts (2..8) that fit
+    splits = sorted({max(1, s0 // 4), max(1, s0 // 2), s0, min(mx, 2 * s0)} | {x for x in (2, 4, 8) if x <= mx})
     return [(w, sp) for w in widths for sp in splits]
 
 

@@ -50,13 +50,14 @@ cudaError_t cg_helper_col2im(const float *cols, float *out, int b, int c, int h,
 cudaError_t cg_helper_transpose(int rows, int cols, const float *in, int ld, float beta, float *out, int kn, int ho,
                                 int wo, int start_row, int start_col, cudaStream_t st);
 
-// Launch with programmatic stream serialization (the kernel must call
-// tc::pdl_wait() before its first global memory access); plain launch when the
-// environment sets CONVGEMM_NO_PDL=1.  Counts the launch.
 bool cg_pdl_enabled();
+
+// Launch, with programmatic stream serialization when `pdl` (and not turned off by
+// CONVGEMM_NO_PDL=1): the kernel must call tc::pdl_wait() before its first global
+// memory access.  Counts the launch.
 template <typename... KArgs, typename... Args>
-cudaError_t cg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                          Args &&...args) {
+cudaError_t cg_launch_ex(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                         Args &&...args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;
@@ -66,8 +67,20 @@ cudaError_t cg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = cg_pdl_enabled() ? 1 : 0;
+    cfg.numAttrs = (pdl && cg_pdl_enabled()) ? 1 : 0;
     cg_note_launch();
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...);
 }
+
+// Launch with programmatic stream serialization (the kernel must call
+// tc::pdl_wait() before its first global memory access); plain launch when the
+// environment sets CONVGEMM_NO_PDL=1.  Counts the launch.
+// Weight-gradient splits as clusters (CONVGEMM_NO_WGRAD_CLUSTER=1 turns it off).
+bool cg_wgrad_cluster_enabled();
+template <typename... KArgs, typename... Args>
+cudaError_t cg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                          Args &&...args) {
+    return cg_launch_ex(true, kernel, grid, block, smem, st, static_cast<Args &&>(args)...);
+}
+
 

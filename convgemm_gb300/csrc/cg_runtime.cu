@@ -34,9 +34,25 @@ convgemm_status_t cg_cuda_check(cudaError_t e, const char *what) {
                         "%s: %s", what, cudaGetErrorString(e));
 }
 
+// Programmatic dependent launch for the persistent chain kernels: per host thread,
+// default on unless the environment sets CONVGEMM_NO_PDL=1.
+static thread_local int tl_pdl = -1;
 bool cg_pdl_enabled() {
-    static const bool on = [] {
+    static const bool env_on = [] {
         const char *e = getenv("CONVGEMM_NO_PDL");
+        return !(e && e[0] == '1');
+    }();
+    return tl_pdl < 0 ? env_on : tl_pdl != 0;
+}
+extern "C" int convgemm_set_pdl(int on) {
+    const int prev = cg_pdl_enabled() ? 1 : 0;
+    tl_pdl = on < 0 ? -1 : (on != 0);
+    return prev;
+}
+
+bool cg_wgrad_cluster_enabled() {
+    static const bool on = [] {
+        const char *e = getenv("CONVGEMM_NO_WGRAD_CLUSTER");
         return !(e && e[0] == '1');
     }();
     return on;

@@ -186,9 +186,10 @@ __global__ void __launch_bounds__(288, 1)
         d.ktiles = c.ktiles; d.tile0 = c.tile0; d.lo_y = c.lo_y; d.lo_x = c.lo_x; d.mint_y = c.mint_y;
         d.mint_x = c.mint_x; d.dwg = c.dwg; d.dhg = c.dhg;
     }
-    // everything above touched only shared memory and kernel parameters
+    // everything above touched only shared memory and kernel parameters; the next kernel may
+    // launch once every CTA has started its last tile (pdl_trigger in the producer loop), so
+    // its waiting CTAs do not hold SMs that work on other streams could use
     tc::pdl_wait();
-    tc::pdl_trigger();
     if (sc_all)
         for (int n = threadIdx.x; n < p.Cout; n += blockDim.x) {
             sc_tab[n] = p.scale ? __ldg(p.scale + n) : 1.0f;
@@ -209,6 +210,7 @@ __global__ void __launch_bounds__(288, 1)
         if (threadIdx.x == 0) {
             uint32_t it = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
+                if (tile + (int) gridDim.x >= p.ntiles_total) tc::pdl_trigger();   // this CTA's last tile
                 const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile, MT);
                 const ClsS &cl = cls_tab[tl.cls];
                 const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;
@@ -264,6 +266,7 @@ __global__ void __launch_bounds__(288, 1)
         const int r0 = t >> 3;     // rows r0 + 16*i
         uint32_t it = 0;
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x) {
+            if (t == 0 && tile + (int) gridDim.x >= p.ntiles_total) tc::pdl_trigger();   // this CTA's last tile
             const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile);
             const ClsS &cl = cls_tab[tl.cls];
             const int32_t *taps = tap_tab + tl.cls * TC_MAXTAPS;

@@ -73,8 +73,7 @@ __global__ void __launch_bounds__(288, 1)
     float *sh_tab = sc_tab + GBN;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    tc::pdl_wait();
-    tc::pdl_trigger();
+    tc::pdl_wait();   // pdl_trigger: when the producer starts this CTA's last tile
     // a table prepared for another count, or a tile count beyond the table: run nothing
     if (__ldg(&probs[0].count) != nprob) {
         if (threadIdx.x == 0) atomicCAS(err, 0, 25);
@@ -108,6 +107,7 @@ __global__ void __launch_bounds__(288, 1)
             uint32_t it = 0;
             int pi = 0;
             for (int tile = blockIdx.x; tile < total && ok; tile += gridDim.x) {
+                if (tile + (int) gridDim.x >= total) tc::pdl_trigger();   // this CTA's last tile
                 pi = advance(probs, nprob, pi, tile);
                 const GroupProblem *P = probs + pi;
                 const int local = tile - __ldg(&P->tile0), ntn = __ldg(&P->ntiles_n), bn = __ldg(&P->bn);

@@ -634,10 +634,11 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.direct = w.splits == 1;
     p.layout = layout == CONVGEMM_NCHW;
     p.C = s.c;
+    p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits);
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
         return e;
-    if (p.direct) return CONVGEMM_SUCCESS;
+    if (p.direct || p.cluster) return CONVGEMM_SUCCESS;
     return cg_cuda_check(tc_wgrad_reduce((float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
                                          s.kw, layout == CONVGEMM_NCHW, st),
                          "weight-gradient reduction");

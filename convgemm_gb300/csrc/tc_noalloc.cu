@@ -162,10 +162,11 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
     p.direct = splits == 1;
     p.layout = layout == CONVGEMM_NCHW;
     p.C = s.c;
+    p.cluster = tc_wgrad_cluster_ok(bn, xa, p.im2col, splits);
     if (convgemm_status_t e =
             cg_cuda_check(tc_wgrad_launch(p, map, xmap, bn, xa, mtiles, ntiles, splits, st), "weight-gradient launch"))
         return e;
-    if (p.direct) return CONVGEMM_SUCCESS;
+    if (p.direct || p.cluster) return CONVGEMM_SUCCESS;
     return cg_cuda_check(
         tc_wgrad_reduce(d->scratch, dw, splits, xa, Nx, s.kn, s.c, Cp, s.kh, s.kw, layout == CONVGEMM_NCHW, st),
         "weight-gradient reduction");

@@ -66,8 +66,7 @@ __global__ void __launch_bounds__(288, 1)
     tc_stem_kernel(const __grid_constant__ StemParams p, const __grid_constant__ CUtensorMap xmap,
                    const __grid_constant__ CUtensorMap wmap) {
     using C = StemCfg<BN>;
-    tc::pdl_wait();   // the weights are loaded in the prologue
-    tc::pdl_trigger();
+    tc::pdl_wait();   // the weights are loaded in the prologue; pdl_trigger: in the producer loop
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint8_t *wres = base + STEM_STAGES * C::STAGE;   // resident weights: K block j at j * B_BYTES
@@ -128,6 +127,7 @@ __global__ void __launch_bounds__(288, 1)
             tma_load_4d(tc::smem_u32(slab), &xmap, 0, -p.pad_w, oy * p.sh - p.pad_h, b, &slab_full[0]);
         }
         for (; tile < p.total && ok; tile += gridDim.x, lt++) {
+            if (t == 0 && tile + (int) gridDim.x >= p.total) tc::pdl_trigger();   // this CTA's last tile
             const int sb = lt & 1;
             // the next tile's slab goes to the other buffer once every producer has read it (tile lt - 1)
             const int nxt = tile + gridDim.x;

@@ -200,7 +200,27 @@ __global__ void __launch_bounds__(160, 1)
         const int m = mrow0 + warp * 32 + lane;
         const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx;
         float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
-        if (ok && p.direct) {
+        if (p.cluster) {
+            // this split's partial tile into shared memory (the ring is idle now), rows padded by
+            // 4 floats against bank conflicts; the cluster adds the splits below
+            float *R = reinterpret_cast<float *>(base);
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t v[32];
+                if (ok) {
+                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+                    tc::tmem_ld_wait();
+                } else {
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj++) v[jj] = 0u;
+                }
+                float4 *dst = reinterpret_cast<float4 *>(R + (size_t) (warp * 32 + lane) * (BN + 4) + c0);
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    dst[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
+                                         __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
+            }
+        } else if (ok && p.direct) {
             // single split: dW written in the reference layout (lanes hold consecutive rows)
             const int khw = p.kh * p.kw;
 #pragma unroll 1
@@ -273,6 +293,57 @@ __global__ void __launch_bounds__(160, 1)
         __syncwarp();
     }
 
+    if (p.cluster) {
+        // dW = sum of the cluster's partial tiles in split (cluster rank) order; rank r adds rows
+        // [r*rows, (r+1)*rows) across all ranks' shared memory and writes them
+        asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+        if (warp < 4) {
+            uint32_t rank, nrank;
+            asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+            asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(nrank));
+            const int rows = (128 + (int) nrank - 1) / (int) nrank, r0 = (int) rank * rows;
+            const int nr = min(rows, 128 - r0);
+            const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx, khw = p.kh * p.kw;
+            const uint32_t Rloc = tc::smem_u32(base);
+            // lanes along rows when rows are dW's contiguous index (co, NHWC layout), else along columns
+            const bool row_fast = !XA && p.layout == 0;
+            for (int e = threadIdx.x; e < nr * (BN / 4); e += 128) {
+                const int rr = row_fast ? e % nr : e / (BN / 4), c4 = row_fast ? e / nr : e % (BN / 4);
+                const int row = r0 + rr;
+                const uint32_t off = (uint32_t) ((row * (BN + 4) + 4 * c4) * 4);
+                float a[4] = {0.f, 0.f, 0.f, 0.f};
+                for (uint32_t z = 0; z < nrank; z++) {
+                    uint32_t ra;
+                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(Rloc + off), "r"(z));
+                    float b0, b1, b2, b3;
+                    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                 : "=f"(b0), "=f"(b1), "=f"(b2), "=f"(b3)
+                                 : "r"(ra)
+                                 : "memory");
+                    a[0] = __fadd_rn(a[0], b0);
+                    a[1] = __fadd_rn(a[1], b1);
+                    a[2] = __fadd_rn(a[2], b2);
+                    a[3] = __fadd_rn(a[3], b3);
+                }
+                const int m = mrow0 + row;
+                if (m >= Mext) continue;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int col = ncol0 + 4 * c4 + q;
+                    if (col >= Next) break;
+                    const int n = XA ? m : col, co = XA ? col : m;
+                    uint32_t tap, ci;
+                    p.dcp.divmod((uint32_t) n, tap, ci);
+                    if ((int) ci >= p.C) continue;
+                    const size_t o = p.layout == 0 ? ((size_t) ci * khw + tap) * p.kn + co
+                                                   : ((size_t) co * p.C + ci) * khw + tap;
+                    p.dw[o] = a[q];
+                }
+            }
+        }
+        // no rank leaves while another still reads its shared memory
+        asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
@@ -374,7 +445,58 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    return cg_launch_pdl(kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
+    // Weight-gradient work runs beside the forward / input-gradient chain on a side
+    // stream: launched without programmatic serialization, so that its grids do not
+    // hold SMs early while the persistent chain kernels want them.
+    if (!p.cluster) return cg_launch_ex(false, kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
+    // the splits of one tile as a cluster along z
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(160);
+    cfg.dynamicSmemBytes = C::SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 1;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = grid.z;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cg_note_launch();
+    return cudaLaunchKernelEx(&cfg, kern, p, map, xmap);
+}
+
+// Whether `splits` CTAs of this configuration can be resident together as one cluster.
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1>
+bool cluster_fits(int splits) {
+    using C = WgCfg<BN, STAGES, XA, KB>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB>;
+    static int cached[9] = {-1, -1, -1, -1, -1, -1, -1, -1, -1};
+    if (splits < 2 || splits > 8) return false;
+    if (cached[splits] < 0) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(1, 1, splits);
+        cfg.blockDim = dim3(160);
+        cfg.dynamicSmemBytes = C::SMEM;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 1;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = splits;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        cached[splits] = n;
+    }
+    return cached[splits] > 0;
 }
 
 // im2col path: two 64-pixel chunks per stage (64-wide tiles: 2 stages of 48 KB, two CTAs
@@ -415,6 +537,21 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
 
 }  // namespace
 
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits) {
+    if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;
+    if (im2col) {
+        if (xa) return bn == 64 ? cluster_fits<64, 2, true, true, 2>(splits)
+                                : bn == 128 && cluster_fits<128, 3, true, true, 2>(splits);
+        return bn == 64    ? cluster_fits<64, 2, false, true, 2>(splits)
+               : bn == 128 ? cluster_fits<128, 3, false, true, 2>(splits)
+                           : bn == 256 && cluster_fits<256, 2, false, true, 2>(splits);
+    }
+    if (xa) return bn == 64 ? cluster_fits<64, 4, true, false>(splits) : bn == 128 && cluster_fits<128, 3, true, false>(splits);
+    return bn == 64    ? cluster_fits<64, 4, false, false>(splits)
+           : bn == 128 ? cluster_fits<128, 3, false, false>(splits)
+                       : bn == 256 && cluster_fits<256, 4, false, false>(splits);
+}
+
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                             int mtiles, int ntiles, int splits, cudaStream_t st) {
     dim3 grid(mtiles, ntiles, splits);
@@ -440,14 +577,14 @@ cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, in
         float *gs = ws + (size_t) splits * plane;
         const int per = (splits + groups - 1) / groups;
         dim3 g1((unsigned) ((plane + 255) / 256), groups);
-        if (cudaError_t e = cg_launch_pdl(wgrad_group_sum_kernel, g1, dim3(256), 0, st, (const float *) ws, gs, splits,
-                                          per, plane))
+        if (cudaError_t e = cg_launch_ex(false, wgrad_group_sum_kernel, g1, dim3(256), 0, st, (const float *) ws, gs, splits,
+                                         per, plane))
             return e;
         src = gs;
         n = groups;
     }
     dim3 grid((kn + 31) / 32, (Nx + 31) / 32), block(32, 8);
-    return cg_launch_pdl(wgrad_reduce_kernel, grid, block, 0, st, src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout);
+    return cg_launch_ex(false, wgrad_reduce_kernel, grid, block, 0, st, src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout);
 }
 
 // ------------------------------------------------------------ bias gradient

@@ -18,11 +18,16 @@ struct TcWgradParams {
     // reference layout `layout` (0: [ci][kh][kw][co], 1: [co][ci][kh][kw]) of C channels
     float *dw;
     int direct, layout, C;
+    // 2..8 splits as one thread-block cluster along z: the partial tiles meet in
+    // distributed shared memory and the cluster writes dW (no workspace, no reduction launch)
+    int cluster;
 };
 
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                             int mtiles, int ntiles, int splits, cudaStream_t st);
+// Whether splits (2..8) can run as clusters for this tile width / operand side.
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits);
 // Split groups of the two-pass reduction (0: one pass).  With many splits, the
 // first pass sums each of G contiguous split ranges into planes that follow the
 // split planes in the workspace, so the workspace holds splits + G planes.

@@ -68,6 +68,13 @@ convgemm_status_t convgemm_selftest_wait_timeout(unsigned budget_ms, void *strea
 /* Number of GPU kernels the library has launched (or recorded into a stream
  * capture) in this process: a diagnostic for counting launches per step. */
 unsigned long long convgemm_launch_count(void);
+/* Programmatic dependent launch of the persistent forward / input-gradient kernels
+ * (a kernel's prologue overlaps the previous kernel's tail on the same stream), for
+ * the calling host thread: 1 on, 0 off, -1 back to the default (on unless the
+ * environment sets CONVGEMM_NO_PDL=1).  Returns the previous setting (0 / 1).
+ * Turn it off while other streams run work beside the chain: the early-launched
+ * CTAs then hold SMs that the other streams' grids would fill. */
+int convgemm_set_pdl(int on);
 const char *convgemm_get_last_error(void);
 void convgemm_clear_error(void);
 /* Reads (and clears) the device-side error word that bounded waits set; it

@@ -106,3 +106,19 @@ def test_tune_table_validation_without_gpu(cglib):
     assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 64, 4) == 1      # splits: weight gradient only
     assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 0, 3) == 0
     tc.tune_clear()
+
+
+def test_set_pdl_is_per_thread_and_restores_default(cglib, monkeypatch):
+    """convgemm_set_pdl switches programmatic launches for the calling thread and
+    returns the previous setting; -1 goes back to the environment's default."""
+    import threading
+    default = 0 if os.environ.get("CONVGEMM_NO_PDL") == "1" else 1
+    assert cglib.set_pdl(0) == default
+    seen = []
+    t = threading.Thread(target=lambda: seen.append(cglib.set_pdl(-1)))
+    t.start()
+    t.join()
+    assert seen == [default]              # another thread still has the default
+    assert cglib.set_pdl(1) == 0
+    assert cglib.set_pdl(-1) == 1
+    assert cglib.set_pdl(-1) == default
