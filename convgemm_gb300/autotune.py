@@ -29,7 +29,7 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
-OP_CACHE_TAG = "v4"   # op entries: fwd / dgrad with the M-tile choice; wgrad with 2-chunk stages, direct single-split writes and 2..8-split clusters
+OP_CACHE_TAG = "v5"   # op entries: fwd / dgrad with the M-tile and epilogue-warp choices; wgrad with 2-chunk stages, direct single-split writes and 2..8-split clusters
 
 
 def cache_path() -> str:
@@ -171,13 +171,25 @@ def graph_time_us(run, reps: int = 10) -> float:
     return a.elapsed_time(b) * 1000 / reps
 
 
+def _mt_ew(widths):
+    """(bn, aux) of the BF16 forward / input gradient: aux = M tiles sharing a weight tile (1 / 2),
+    + 4 for eight epilogue warps (bn >= 128 or two M tiles, not bn 256 with two)."""
+    out = []
+    for w in widths:
+        for m in (1, 2):
+            out.append((w, m))
+            if (w >= 128 or m == 2) and not (w == 256 and m == 2):
+                out.append((w, m + 4))
+    return out
+
+
 def op_candidates(op: int, s):
-    """(bn, aux) candidates: aux = weight-gradient pixel splits, or M tiles (1 / 2) sharing each
-    weight tile of the BF16 forward / input gradient; 0 = heuristic."""
-    if op == tc.TUNE_DGRAD:   # second value: M tiles sharing a weight tile
-        return [(w, m) for w in candidate_widths(s.c) for m in (1, 2)]
+    """(bn, aux) candidates: aux = weight-gradient pixel splits, or for the BF16 forward / input
+    gradient the M tiles (1 / 2) sharing each weight tile, + 4 for eight epilogue warps."""
+    if op == tc.TUNE_DGRAD:
+        return _mt_ew(candidate_widths(s.c))
     if op == tc.TUNE_FWD:
-        return [(w, m) for w in candidate_widths(s.kn) for m in (1, 2)]
+        return _mt_ew(candidate_widths(s.kn))
     if op != tc.TUNE_WGRAD:
         return [(w, 0) for w in candidate_widths(s.kn)]
     tc.tune_set(op, s, 0, 0)

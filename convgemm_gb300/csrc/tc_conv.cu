@@ -48,7 +48,10 @@ constexpr int MODE_X3 = 2;    // 3xBF16: hi*hi + hi*lo + lo*hi into one accumula
 // MT 128-row M tiles share every weight tile: each K block loads MT activation
 // tiles and one weight tile and issues MT MMAs into MT accumulators, which cuts
 // the shared-memory bytes per FLOP (the operand delivery from L2 bounds the kernel).
-template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16, int MT = 1>
+// EW epilogue warps: 4 (one per TMEM lane quarter), or 8 (two per quarter, taking
+// alternate 64-column chunks) for short-K tiles, whose time goes to the epilogue's
+// latency chain (TMEM load, scale/shift, convert, staging) rather than the MMAs.
+template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16, int MT = 1, int EW = 4>
 struct TcCfg {
     static constexpr int BM = 128, BK = 64;            // K elements per block
     static constexpr int ROWB = MODE == MODE_FP8 ? 64 : 128;  // bytes of one K row of a block
@@ -64,7 +67,7 @@ struct TcCfg {
     static constexpr uint32_t LAYOUT = ROWB == 128 ? 2 : 4;    // SWIZZLE_128B / SWIZZLE_64B
     static constexpr bool OUTF32 = MODE == MODE_X3;
     static constexpr int CW = OUTF32 ? 32 : 64;                // output columns per 128-byte staging row
-    static constexpr uint32_t EPI_BYTES = BM * 128;            // one 128-row output chunk
+    static constexpr uint32_t EPI_BYTES = EW * 32 * 128;       // one 32-row x 128-byte chunk per epilogue warp
     // cp.async groups in flight per producer thread; the other STAGES - LAG slots let the
     // MMA run ahead of the arrivals (LAG = STAGES - 1 would lock the two in step)
     static constexpr int LAG = STAGES / 2;
@@ -75,7 +78,12 @@ struct TcCfg {
         (1024 + (size_t) STAGES * STAGE_BYTES + 2 * EPI_BYTES + 256 + TAB_BYTES <= 232448) ? 2 : 1;
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + EPI_BUFS * EPI_BYTES + 256 + TAB_BYTES;
     static_assert(SMEM <= 232448, "shared memory above the 227 KB per-block limit");
-    static constexpr int THREADS = 288;
+    static_assert(EW == 4 || EW == 8, "four or eight epilogue warps");
+    // warps: 0 producer (0-3 on the cp.async path), 4..4+EW-1 epilogue, the MMA issuer in
+    // warp 8 (EW = 4) or in the otherwise idle warp 1 (EW = 8)
+    static constexpr int THREADS = EW == 8 ? 384 : 288;
+    static constexpr int MMA_WARP = EW == 8 ? 1 : 8;
+    static constexpr int NCH = BN / CW;   // output chunks of one accumulator
     // TMEM: MT accumulators of BN columns, double-buffered when 512 columns allow
     static constexpr int ACC_BUFS = 2 * BN * MT <= 512 ? 2 : 1;
     static constexpr uint32_t TMEM_COLS = ACC_BUFS * BN * MT;
@@ -92,7 +100,8 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"((uint64_t) map),
@@ -130,11 +139,12 @@ __device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntile
     return tl;
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT>
-__global__ void __launch_bounds__(288, 1)
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT, int EW>
+__global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
-    using C = TcCfg<BN, STAGES, KB, MODE, MT>;
+    using C = TcCfg<BN, STAGES, KB, MODE, MT, EW>;
+    static_assert(EW == 4 || (IM2C && MT * C::NCH >= 2), "eight epilogue warps: im2col path, two chunks or more");
     static_assert(IM2C || (KB == 1 && MODE == MODE_BF16), "the cp.async gather fills one BF16 K block per stage");
     static_assert(MT == 1 || (IM2C && MODE == MODE_BF16), "two M tiles per weight tile: BF16 im2col path only");
     extern __shared__ uint8_t smem_raw[];
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(288, 1)
         }
         for (int b = 0; b < 2; b++) {
             tc::mbar_init(&acc_full[b], 1);
-            tc::mbar_init(&acc_empty[b], 128);
+            tc::mbar_init(&acc_empty[b], 32 * EW);
         }
         tc::fence_mbar_init();
         tc::prefetch_tmap(&wmap);
@@ -195,7 +205,7 @@ __global__ void __launch_bounds__(288, 1)
             sc_tab[n] = p.scale ? __ldg(p.scale + n) : 1.0f;
             sh_tab[n] = p.shift ? __ldg(p.shift + n) : 0.0f;
         }
-    if (warp == 8) {
+    if (warp == C::MMA_WARP) {
         tc::tmem_alloc(tmem_holder, C::TMEM_COLS);
         tc::tmem_relinquish();
     }
@@ -205,7 +215,7 @@ __global__ void __launch_bounds__(288, 1)
     const uint32_t tmem = *tmem_holder;
     bool ok = true;
 
-    if (IM2C && warp < 4) {
+    if (IM2C && warp < 4 && warp != C::MMA_WARP) {
         // ------------------------------------------------ producer: one thread, im2col TMA for A, TMA for B
         if (threadIdx.x == 0) {
             uint32_t it = 0;
@@ -259,7 +269,7 @@ __global__ void __launch_bounds__(288, 1)
                 }
             }
         }
-    } else if (warp < 4) {
+    } else if (!IM2C && warp < 4) {
         // ------------------------------------------------ producers: gather A, TMA B
         const int t = threadIdx.x;
         const int piece = t & 7;   // 16-byte piece of the 128-byte K row
@@ -325,11 +335,13 @@ __global__ void __launch_bounds__(288, 1)
         tc::fence_proxy_async_smem();
         if (ok)
             for (uint32_t j = (it > (uint32_t) C::LAG ? it - C::LAG : 0); j < it; j++) tc::mbar_arrive(&full[j % STAGES]);
-    } else if (warp < 8) {
+    } else if (warp >= 4 && warp < 4 + EW) {
         // ------------------------------------------------ epilogue
-        const int ew = warp - 4;          // TMEM lane quarter
+        const int ew = (warp - 4) & 3;    // TMEM lane quarter (a warp reads lanes 32 * (warp % 4) ..)
+        const int half = (warp - 4) >> 2; // EW = 8: which alternate chunks this warp takes
         const int row = ew * 32 + lane;   // tile row = TMEM lane
-        const int et = threadIdx.x - 128; // 0..127
+        const int et = threadIdx.x - 128; // 0 .. 32 * EW - 1
+        uint8_t *const stg_warp = epi_smem + (warp - 4) * 4096;   // this warp's 32 x 128-byte staging
         uint32_t lt = 0;                  // local tile count
         int ebuf = 0;                     // staging buffer toggle
         for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
@@ -343,38 +355,42 @@ __global__ void __launch_bounds__(288, 1)
                 shp += tl.n0;
             } else {
                 // this tile's scale/shift (the previous tile's readers passed the barrier below)
-                epi_bar();
-                for (int j = et; j < BN; j += 128) {
+                epi_bar<32 * EW>();
+                for (int j = et; j < BN; j += 32 * EW) {
                     const int n = min(tl.n0 + j, p.Cout - 1);
                     sc_tab[j] = p.scale ? __ldg(p.scale + n) : 1.0f;
                     sh_tab[j] = p.shift ? __ldg(p.shift + n) : 0.0f;
                 }
-                epi_bar();
+                epi_bar<32 * EW>();
             }
             ok = tc::mbar_wait(&acc_full[buf], (lt / C::ACC_BUFS) & 1, p.err, 3);
             if (!ok) break;
             tc::tc_fence_after();
+            // items: (accumulator mt, chunk c0) in order; with eight warps the two warps of a
+            // lane quarter take alternate items
+            constexpr int NIT = MT * C::NCH, STEP = EW / 4;
 #pragma unroll 1
-          for (int mt = 0; mt < MT; mt++) {
-            const int m0 = tl.m0 + mt * 128;   // this accumulator's first output row
-            const int m = m0 + row;
-            uint8_t *orow = nullptr;   // this row of the output (BF16, or FP32 for MODE_X3)
-            if (!p.epi_tma && m < M) {
-                uint32_t q, jw, j, b;
-                cl.dwg.divmod(m, q, jw);
-                cl.dhg.divmod(q, b, j);
-                const int oy = cl.oy0 + cl.osy * (int) j, ox = cl.ox0 + cl.osx * (int) jw;
-                orow = (uint8_t *) p.out + ((((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout) * (C::OUTF32 ? 4 : 2);
-            }
-#pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += C::CW) {
+            for (int item = half; item < NIT; item += STEP) {
+                const int mt = item / C::NCH, c0 = (item % C::NCH) * C::CW;
+                const int m0 = tl.m0 + mt * 128;   // this accumulator's first output row
+                const int m = m0 + row;
+                uint8_t *orow = nullptr;   // this row of the output (BF16, or FP32 for MODE_X3)
+                if (!p.epi_tma && m < M) {
+                    uint32_t q, jw, j, b;
+                    cl.dwg.divmod(m, q, jw);
+                    cl.dhg.divmod(q, b, j);
+                    const int oy = cl.oy0 + cl.osy * (int) j, ox = cl.ox0 + cl.osx * (int) jw;
+                    orow = (uint8_t *) p.out +
+                           ((((size_t) b * p.Hout + oy) * p.Wout + ox) * p.Cout) * (C::OUTF32 ? 4 : 2);
+                }
                 uint32_t v0[32], v1[32];
                 const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) ((buf * MT + mt) * BN + c0);
                 tc::tmem_ld_32x32b_x32(ta, v0);
                 if (C::CW == 64) tc::tmem_ld_32x32b_x32(ta + 32, v1);
                 tc::tmem_ld_wait();
-                if (mt == MT - 1 && c0 + C::CW >= BN) {
-                    // the whole accumulator is in registers: hand the TMEM buffer back to the MMA warp
+                if (item + STEP >= NIT) {
+                    // this warp's last read of the accumulator: its share of the TMEM buffer
+                    // goes back to the MMA warp
                     tc::tc_fence_before();
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
@@ -427,7 +443,7 @@ __global__ void __launch_bounds__(288, 1)
                         else bulk_wait_read<0>();
                     }
                     __syncwarp();
-                    uint8_t *stg = epi_smem + ebuf * C::EPI_BYTES + ew * (C::EPI_BYTES / 4);
+                    uint8_t *stg = stg_warp + ebuf * C::EPI_BYTES;
 #pragma unroll
                     for (int q = 0; q < 8; q++) {
                         uint4 u = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
@@ -461,7 +477,6 @@ __global__ void __launch_bounds__(288, 1)
                     }
                 }
             }
-          }
         }
         if (lane == 0) bulk_wait_all();
     } else {
@@ -527,14 +542,14 @@ __global__ void __launch_bounds__(288, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 8) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+    if (warp == C::MMA_WARP) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT = 1>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT = 1, int EW = 4>
 cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
                       int grid, cudaStream_t st) {
-    using C = TcCfg<BN, STAGES, KB, MODE, MT>;
-    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE, MT>;
+    using C = TcCfg<BN, STAGES, KB, MODE, MT, EW>;
+    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE, MT, EW>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -565,6 +580,21 @@ cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const
             case 64: return launch_bn<64, 4, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
             case 128: return launch_bn<128, 3, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
             case 256: return launch_bn<256, 2, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (p.im2col && p.ew == 8) {
+        // eight epilogue warps (short-K tiles): one K block per stage, two staging buffers
+        if (p.mt == 2) {
+            switch (p.bn) {
+                case 64: return launch_bn<64, 3, 1, true, MODE_BF16, 2, 8>(p, wmap, omap, amaps, grid, st);
+                case 128: return launch_bn<128, 3, 1, true, MODE_BF16, 2, 8>(p, wmap, omap, amaps, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        switch (p.bn) {
+            case 128: return launch_bn<128, 4, 1, true, MODE_BF16, 1, 8>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 1, true, MODE_BF16, 1, 8>(p, wmap, omap, amaps, grid, st);
             default: return cudaErrorInvalidValue;
         }
     }

@@ -46,6 +46,7 @@ struct TcConvParams {
     int cpb;                   // 64-channel chunks per tap (Cin / 64) on the im2col path
     int mode;                  // 0 BF16, 1 FP8-E4M3, 2 3xBF16 (FP32 output)
     int mt;                    // 128-row M tiles per tile (1, or 2 sharing each weight tile: BF16 im2col only)
+    int ew;                    // epilogue warps: 4, or 8 (BF16 im2col, bn >= 128 or mt == 2, not bn 256 with mt 2)
     int ncls;
     TcClass cls[TC_MAXCLS];
 };

@@ -58,19 +58,26 @@ EncodeIm2colFn encode_im2col_fn() {
 
 // im2col-mode map of a BF16 NHWC tensor [B][H][W][C]: `pixels` pixels x 64 channels per load,
 // bounding box [lo, dim-1+up] per spatial dimension, traversal strides (sh, sw), 128-byte swizzle.
-convgemm_status_t tc_make_map_4d_box(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int box_h,
-                                     int box_w) {
+convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, const unsigned long long *dims,
+                                  const unsigned long long *strides_bytes, const unsigned *box, const unsigned *estr,
+                                  int swizzle128) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    if (((uintptr_t) ptr & 15) || (C * 2) % 16)
-        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA operand not 16-byte aligned");
-    cuuint64_t dims[4] = {(cuuint64_t) C, (cuuint64_t) W, (cuuint64_t) H, (cuuint64_t) B};
-    cuuint64_t strides[3] = {(cuuint64_t) C * 2, (cuuint64_t) W * C * 2, (cuuint64_t) H * W * C * 2};
-    cuuint32_t box[4] = {(cuuint32_t) C, (cuuint32_t) box_w, (cuuint32_t) box_h, 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(ptr), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if ((uintptr_t) ptr & 15) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA operand not 16-byte aligned");
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], e[5];
+    for (int i = 0; i < rank; i++) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        e[i] = estr[i];
+        if (i < rank - 1) {
+            st[i] = strides_bytes[i];
+            if (st[i] % 16) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA stride not a multiple of 16 bytes");
+        }
+    }
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t) rank, const_cast<void *>(ptr), d, st, b, e,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int) r);
     return CONVGEMM_SUCCESS;
 }
@@ -294,7 +301,7 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
-                         const void *in_lo, const void *w_lo, int bn_override, int mt_override,
+                         const void *in_lo, const void *w_lo, int bn_override, int aux_override,
                          const void *mask) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
@@ -364,8 +371,17 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
                     tc_make_map_2d(&amaps.wlo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, w_lo, pl.Cout, pl.Ktot, 64, p.bn))
                 return e;
     }
-    // two M tiles per weight tile only on the BF16 im2col path
-    p.mt = (mt_override == 2 && mode == 0 && p.im2col) ? 2 : 1;
+    // aux (tuning): bits 0-1 the M tiles per weight tile (1 / 2: BF16 im2col path only), bit 2
+    // eight epilogue warps; 0 = heuristic: one M tile, eight epilogue warps when every class
+    // has at most 8 K blocks per tile (the epilogue, not the MMA, bounds such tiles)
+    p.mt = ((aux_override & 3) == 2 && mode == 0 && p.im2col) ? 2 : 1;
+    bool ew8 = (aux_override & 4) != 0;
+    if (aux_override == 0) {
+        int kmax = 0;
+        for (int c = 0; c < pl.ncls; c++) kmax = pl.cls[c].ktiles > kmax ? pl.cls[c].ktiles : kmax;
+        ew8 = kmax <= 8;
+    }
+    p.ew = (ew8 && mode == 0 && p.im2col && (p.bn >= 128 || p.mt == 2) && !(p.bn == 256 && p.mt == 2)) ? 8 : 4;
     int t0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
         p.cls[c] = pi.cls[c];
@@ -464,7 +480,8 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     tc_plan_fwd(s, pl);
-    if (tc_stem_applicable(s))   // c <= 8, output rows of <= 128 pixels: input slabs staged in shared memory
+    // c <= 8: MMA operands read straight from input slabs in shared memory
+    if (tc_stem_applicable(s) && !((uintptr_t) y & 15) && !((uintptr_t) wpacked & 15) && !((uintptr_t) x & 15))
         return tc_stem_run(s, x, wpacked, pl.Ktot, y, scale, shift, relu, (cudaStream_t) stream);
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_FWD, *shape, &t);

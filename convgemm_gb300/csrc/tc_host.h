@@ -25,10 +25,12 @@ convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, in
                                     long long rows, long long cols, int box_cols, int box_rows, CUtensorMapSwizzle sw);
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
                                      int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
-// 4-D NHWC BF16 map [B][H][W][C] with a {C, box_w, box_h, 1} box, no swizzle.
-convgemm_status_t tc_make_map_4d_box(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int box_h,
-                                     int box_w);
 bool tc_plan_im2col(TcPlan &pl);
+// BF16 tiled tensor map of any rank (<= 5): dims / box / element strides innermost first,
+// strides_bytes of dims 1.. ; 128-byte swizzle or none.
+convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, const unsigned long long *dims,
+                                  const unsigned long long *strides_bytes, const unsigned *box, const unsigned *estr,
+                                  int swizzle128);
 // Forward of convolutions with at most 8 input channels (tc_stem.cu).
 bool tc_stem_applicable(const cg_shape &s);
 convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,
@@ -47,4 +49,4 @@ bool tc_tune_get(int op, const convgemm_shape_t &s, TcTune *t);
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,
                          const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0,
-                         int mt_override = 0, const void *mask = nullptr);
+                         int aux_override = 0, const void *mask = nullptr);

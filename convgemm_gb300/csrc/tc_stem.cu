@@ -1,21 +1,37 @@
-// BF16 forward of convolutions with at most 8 input channels whose output rows
-// fit one 128-row tile (the 7x7/s2 ResNet stem on 224x224 input, the first
-// layers of VGG-like networks): sconvGemmNHWC('N') (src/convGemm.c:65-70) for c <= 8.
+// BF16 forward of convolutions with at most 8 input channels (the 7x7/s2 ResNet
+// stem on 224x224 input, the first layer of VGG-like networks):
+// sconvGemmNHWC('N') (src/convGemm.c:65-70) for c <= 8.
 //
-// With c padded to 8 one tap of one pixel is 16 bytes, and the general kernel's
-// im2row gather issues one 16-byte cp.async per (pixel, tap): the load-store
-// unit, not memory, bounds it.  Here a tile is one output row (b, oy) of up to
-// 128 pixels:
-//   * one TMA load brings the input slab the row needs -- Hbox = (kh-1)*dh + 1
-//     input rows x Wbox = (wo-1)*sw + (kw-1)*dw + 1 pixels x 8 channels, zero
-//     outside the image -- into shared memory (double-buffered across tiles);
-//   * the 128 producer threads build each 64-deep K block (8 taps x 8 channels)
-//     of the 128-byte-swizzled K-major A tile from the slab with 16-byte
-//     shared-memory copies (taps past kh*kw and rows past wo are zero);
-//   * the packed weights of the (single) N tile are loaded once per CTA and stay
-//     resident; a pipeline stage carries two K blocks of A;
-//   * tcgen05.mma accumulates in TMEM, and the epilogue applies scale / shift /
-//     ReLU and stores each valid row directly.
+// With c padded to 8 one tap of one pixel is 16 bytes: too narrow for im2col-mode
+// TMA (one 16-byte request per pixel and tap) and, copied into 128-byte-swizzled
+// A tiles by threads, bound by shared-memory copies.  Here the tensor core reads
+// its A operand straight out of input slabs:
+//   * a tile is a chunk of up to 128 output pixels of one output row (b, oy,
+//     columns 128*wc ..);
+//   * for each residue rho of the input column modulo the horizontal stride sw,
+//     one TMA load (traversal stride sw along W) brings the slab
+//     S_rho[i][j] = x[b][oy*sh - pad_h + i][sw*(128*wc + qmin + j) + rho][0..7]
+//     for i < Hbox = (kh-1)*dh + 1 input rows: tap (ky, kx), whose input column
+//     for output column ox is sw*(ox + q) + rho with kx*dw - pad_w = sw*q + rho,
+//     reads rows j = r + q - qmin of S_rho[ky*dh] for the tile's pixels r -- 128
+//     consecutive 16-byte rows, i.e. a K-major operand of 8 K elements in the
+//     no-swizzle core-matrix layout (8 rows x 16 bytes, 8-row groups 128 bytes
+//     apart);
+//   * one kind::f16 MMA (K = 16) takes two taps: the descriptor's leading-dimension
+//     byte offset (the K-direction core-matrix stride) is the distance between the
+//     two taps' slab rows, so taps are paired in address order; an odd last tap is
+//     paired with a 2 KB zero region behind each slab buffer (which also absorbs
+//     the reads of rows past the chunk's valid pixels);
+//   * the packed weights of the single N tile are resident in shared memory in the
+//     same pair order: pair p holds [BN][8] BF16 for its first tap, then for its
+//     second (zero for the zero region);
+//   * slab buffers are double-buffered across tiles: the MMA commit of a tile frees
+//     its slab, the next-but-one tile's TMA loads refill it;
+//   * the epilogue applies scale / shift / ReLU and stores through per-warp TMA
+//     stores of a 3-D output map [B*Ho][Wo][kn] (rows past Wo are clipped).
+// There is no K pipeline: the whole reduction of a tile (kh*kw*8 <= 512 deep) is
+// one slab.
+#include <algorithm>
 #include <cstring>
 
 #include <cuda_bf16.h>
@@ -27,30 +43,44 @@
 
 namespace {
 
-constexpr int STEM_STAGES = 3;
-constexpr int STEM_KB = 2;                       // K blocks per stage
-constexpr uint32_t STEM_A = 128 * 128;           // one K block: 128 rows x 64 BF16 K
-constexpr uint32_t STEM_SLAB_MAX = 27 * 1024;   // input slab bytes per buffer
-constexpr uint32_t STEM_W_MAX = 64 * 1024;      // resident packed weights (every K block of the N tile)
 constexpr int STEM_MAXTAPS = 64;
+constexpr int STEM_MAXPAIRS = STEM_MAXTAPS / 2;
+constexpr uint32_t STEM_SLAB_MAX = 48 * 1024;    // the residue slabs of one buffer
+constexpr uint32_t STEM_ZERO = 2048;             // zero region behind each slab buffer: 128 rows x 16 B
+constexpr uint32_t STEM_W_MAX = 64 * 1024;       // resident weights
+constexpr uint32_t STEM_EPI = 4 * 4096;          // per-warp output staging, 32 rows x 128 B
 
 struct StemParams {
-    __nv_bfloat16 *out;
+    const __nv_bfloat16 *w;   // packed weights [kn][Kpad], K = tap * 8 + channel
     const float *scale, *shift;
-    int relu, B, Ho, Wo, kn, ntaps, ktiles, ntn, total, sw, Wbox, Hbox, pad_h, pad_w, sh;
+    int relu, B, Ho, Wo, kn, Kpad, nwc, total, sh, sw, pad_h, qmin, npairs;
+    uint32_t buf_bytes;       // one slab buffer: sw residue slabs (rho_bytes apart) + the zero region
+    uint32_t rho_bytes;       // one residue slab, 1024-aligned
+    uint32_t slab_tx;         // bytes the TMA loads of one tile deliver
     int *err;
-    int32_t tapoff[STEM_MAXTAPS];   // slab pixel offset of each tap for output column 0
+    uint32_t aoff[STEM_MAXPAIRS];   // byte offset of the pair's first tap rows within a slab buffer
+    uint32_t alead[STEM_MAXPAIRS];  // bytes from the first to the second tap's rows (or to the zero region)
+    int16_t wtap[2 * STEM_MAXPAIRS];   // the pair's taps (ky * kw + kx) in the packed weights; -1 = zero
 };
 
 template <int BN>
 struct StemCfg {
-    static constexpr uint32_t B_BYTES = BN * 128;   // one K block of weights
-    static constexpr uint32_t STAGE = STEM_KB * STEM_A;
-    static constexpr size_t SMEM = 1024 + (size_t) STEM_STAGES * STAGE + STEM_W_MAX + 2 * (size_t) STEM_SLAB_MAX + 256 +
-                                   2 * BN * 4 + STEM_MAXTAPS * 4;   // 256: the mbarriers
+    static constexpr uint32_t PAIR_W = 2 * BN * 16;   // one pair of taps of the resident weights
+    static constexpr size_t SMEM = 1024 + (size_t) STEM_W_MAX + 2 * ((size_t) STEM_SLAB_MAX + STEM_ZERO) +
+                                   2 * STEM_EPI + 256 + 2 * BN * 4 + 2 * STEM_MAXPAIRS * 4;
     static_assert(SMEM <= 232448, "shared memory");
 };
 
+// No-swizzle K-major descriptor: core matrices of 8 rows x 16 bytes; `lead` = bytes
+// between the core matrices of K elements 0-7 and 8-15, 8-row groups 128 bytes apart.
+__device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t lead) {
+    uint64_t d = 0;
+    d |= (uint64_t) ((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t) ((lead >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t) (128 >> 4) << 32;
+    d |= (uint64_t) 1 << 46;   // descriptor version for tcgen05; layout bits 61-63 = 0: no swizzle
+    return d;
+}
 
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
                                             uint64_t *bar) {
@@ -61,51 +91,81 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int c0, int c1, int c2) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                     (uint64_t) map),
+                 "r"(src), "r"(c0), "r"(c1), "r"(c2)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+
 template <int BN>
 __global__ void __launch_bounds__(288, 1)
     tc_stem_kernel(const __grid_constant__ StemParams p, const __grid_constant__ CUtensorMap xmap,
-                   const __grid_constant__ CUtensorMap wmap) {
+                   const __grid_constant__ CUtensorMap omap) {
     using C = StemCfg<BN>;
-    tc::pdl_wait();   // the weights are loaded in the prologue; pdl_trigger: in the producer loop
+    tc::pdl_wait();   // weights and input may come from the previous kernel; pdl_trigger: producer's last tile
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-    uint8_t *wres = base + STEM_STAGES * C::STAGE;   // resident weights: K block j at j * B_BYTES
-    uint8_t *slab = wres + STEM_W_MAX;                // two buffers of STEM_SLAB_MAX (1024-aligned)
-    uint64_t *full = (uint64_t *) (slab + 2 * STEM_SLAB_MAX);
-    uint64_t *empty = full + STEM_STAGES;
-    uint64_t *slab_full = empty + STEM_STAGES;
+    uint8_t *wres = base;                                   // resident weights, pair p at p * PAIR_W
+    uint8_t *slab = wres + STEM_W_MAX;                      // two buffers of p.buf_bytes (1024-aligned)
+    uint8_t *epi = slab + 2 * (STEM_SLAB_MAX + STEM_ZERO);  // 2 x 4 warps x 4 KB of output staging
+    uint64_t *slab_full = (uint64_t *) (epi + 2 * STEM_EPI);
     uint64_t *slab_free = slab_full + 2;
     uint64_t *acc_full = slab_free + 2;
     uint64_t *acc_empty = acc_full + 2;
-    uint64_t *wfull = acc_empty + 2;
-    uint32_t *tmem_holder = (uint32_t *) (wfull + 1);
-    float *sc_tab = (float *) (slab + 2 * STEM_SLAB_MAX + 256);
+    uint32_t *tmem_holder = (uint32_t *) (acc_empty + 2);
+    float *sc_tab = (float *) (epi + 2 * STEM_EPI + 256);
     float *sh_tab = sc_tab + BN;
-    int32_t *tap_tab = (int32_t *) (sh_tab + BN);
+    uint32_t *aoff_tab = (uint32_t *) (sh_tab + BN);
+    uint32_t *alead_tab = aoff_tab + STEM_MAXPAIRS;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t slab_bytes = (uint32_t) p.Hbox * p.Wbox * 16;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STEM_STAGES; s++) {
-            tc::mbar_init(&full[s], 4);   // the 4 A-builder warps
-            tc::mbar_init(&empty[s], 1);
-        }
         for (int b = 0; b < 2; b++) {
             tc::mbar_init(&slab_full[b], 1);
-            tc::mbar_init(&slab_free[b], 4);   // every producer warp done reading the buffer
+            tc::mbar_init(&slab_free[b], 1);   // the MMA commit of the tile that read the buffer
             tc::mbar_init(&acc_full[b], 1);
             tc::mbar_init(&acc_empty[b], 128);
         }
-        tc::mbar_init(wfull, 1);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&xmap);
-        // the whole N tile of packed weights (the path takes one N tile), loaded once
-        tc::mbar_arrive_expect_tx(wfull, p.ktiles * C::B_BYTES);
-        for (int j = 0; j < p.ktiles; j++)
-            tc::tma_load_2d(tc::smem_u32(wres + j * C::B_BYTES), &wmap, j * 64, 0, wfull);
+        tc::prefetch_tmap(&omap);
     }
-    for (int i = threadIdx.x; i < STEM_MAXTAPS; i += blockDim.x) tap_tab[i] = i < p.ntaps ? p.tapoff[i] : 0;
-    if (warp == 8) {
+    if (warp < 4) {
+        // the resident weights in pair order, and the zero regions
+        const int t = threadIdx.x;
+        const int nrow = p.npairs * 2 * BN;   // 16-byte rows
+        for (int i = t; i < nrow; i += 128) {
+            const int half = i / BN, n = i % BN;   // half = 2 * pair + (second tap)
+            const int tap = p.wtap[half];
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (tap >= 0 && n < p.kn)
+                v = __ldg(reinterpret_cast<const uint4 *>(p.w + (size_t) n * p.Kpad + tap * 8));
+            *reinterpret_cast<uint4 *>(wres + (size_t) i * 16) = v;
+        }
+        for (int b = 0; b < 2; b++)
+            for (int i = t; i < (int) (STEM_ZERO / 16); i += 128)
+                *reinterpret_cast<uint4 *>(slab + b * p.buf_bytes + p.sw * p.rho_bytes + i * 16) =
+                    make_uint4(0, 0, 0, 0);
+        tc::fence_proxy_async_smem();
+    } else if (warp < 8) {
+        const int et = threadIdx.x - 128;
+        for (int n = et; n < BN; n += 128) {
+            const int nn = min(n, p.kn - 1);
+            sc_tab[n] = p.scale ? __ldg(p.scale + nn) : 1.0f;
+            sh_tab[n] = p.shift ? __ldg(p.shift + nn) : 0.0f;
+        }
+        for (int i = et; i < p.npairs; i += 128) {
+            aoff_tab[i] = p.aoff[i];
+            alead_tab[i] = p.alead[i];
+        }
+    } else {
         tc::tmem_alloc(tmem_holder, 2 * BN);
         tc::tmem_relinquish();
     }
@@ -115,80 +175,35 @@ __global__ void __launch_bounds__(288, 1)
     const uint32_t tmem = *tmem_holder;
     bool ok = true;
 
-    if (warp < 4) {
-        // ------------------------------------------------ producers: slab TMA, A builds, weights TMA
-        const int t = threadIdx.x;
-        const int tt = t & 7, r0 = t >> 3;   // this thread's tap within a K block; rows r0 + 16*i
-        uint32_t it = 0, lt = 0;
-        int tile = blockIdx.x;
-        if (t == 0 && tile < p.total) {
-            const int row = tile / p.ntn, b = row / p.Ho, oy = row % p.Ho;
-            tc::mbar_arrive_expect_tx(&slab_full[0], slab_bytes);
-            tma_load_4d(tc::smem_u32(slab), &xmap, 0, -p.pad_w, oy * p.sh - p.pad_h, b, &slab_full[0]);
-        }
-        for (; tile < p.total && ok; tile += gridDim.x, lt++) {
-            if (t == 0 && tile + (int) gridDim.x >= p.total) tc::pdl_trigger();   // this CTA's last tile
-            const int sb = lt & 1;
-            // the next tile's slab goes to the other buffer once every producer has read it (tile lt - 1)
-            const int nxt = tile + gridDim.x;
-            if (t == 0 && nxt < p.total) {
-                if (lt >= 1 && !(ok = tc::mbar_wait(&slab_free[sb ^ 1], ((lt - 1) >> 1) & 1, p.err, 46))) break;
-                const int nrow = nxt / p.ntn, nb = nrow / p.Ho, noy = nrow % p.Ho;
-                tc::mbar_arrive_expect_tx(&slab_full[sb ^ 1], slab_bytes);
-                tma_load_4d(tc::smem_u32(slab + (sb ^ 1) * STEM_SLAB_MAX), &xmap, 0, -p.pad_w, noy * p.sh - p.pad_h,
-                            nb, &slab_full[sb ^ 1]);
+    if (warp == 0) {
+        // ------------------------------------------------ producer: the slab TMA loads of each tile
+        if (lane == 0) {
+            uint32_t lt = 0;
+            for (int tile = blockIdx.x; tile < p.total && ok; tile += gridDim.x, lt++) {
+                if (tile + (int) gridDim.x >= p.total) tc::pdl_trigger();   // this CTA's last tile
+                const int sb = lt & 1;
+                if (lt >= 2 && !(ok = tc::mbar_wait(&slab_free[sb], ((lt >> 1) + 1) & 1, p.err, 41))) break;
+                const int row = tile / p.nwc, wc = tile % p.nwc;
+                const int b = row / p.Ho, oy = row % p.Ho;
+                const uint32_t dst = tc::smem_u32(slab + sb * p.buf_bytes);
+                tc::mbar_arrive_expect_tx(&slab_full[sb], p.slab_tx);
+                for (int rho = 0; rho < p.sw; rho++)
+                    tma_load_4d(dst + rho * p.rho_bytes, &xmap, 0, p.sw * (128 * wc + p.qmin) + rho,
+                                oy * p.sh - p.pad_h, b, &slab_full[sb]);
             }
-            if (!(ok = tc::mbar_wait(&slab_full[sb], (lt >> 1) & 1, p.err, 41))) break;
-            const uint8_t *sl = slab + sb * STEM_SLAB_MAX;
-            for (int j0 = 0; j0 < p.ktiles; j0 += STEM_KB, it++) {
-                const int s = it % STEM_STAGES;
-                const uint32_t ph = (it / STEM_STAGES) & 1;
-                if (it >= (uint32_t) STEM_STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 42))) break;
-                for (int kb = 0; kb < STEM_KB && j0 + kb < p.ktiles; kb++) {
-                    uint8_t *A = base + s * C::STAGE + kb * STEM_A;
-                    const int tap = (j0 + kb) * 8 + tt;
-                    const bool tap_ok = tap < p.ntaps;
-                    const int toff = tap_ok ? tap_tab[tap] : 0;
-#pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        const int r = r0 + 16 * i;
-                        uint4 v = make_uint4(0, 0, 0, 0);
-                        if (tap_ok && r < p.Wo) v = *reinterpret_cast<const uint4 *>(sl + (size_t) (toff + r * p.sw) * 16);
-                        *reinterpret_cast<uint4 *>(A + r * 128 + ((tt ^ (r & 7)) << 4)) = v;
-                    }
-                }
-                tc::fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&full[s]);   // one arrival per warp: its 32 rows are written
-            }
-            __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&slab_free[sb]);   // the warp's reads of the slab are done
         }
-    } else if (warp < 8) {
-        // ------------------------------------------------ epilogue: direct stores of the valid rows
-        const int ew = warp - 4, r = ew * 32 + lane, et = threadIdx.x - 128;
+        __syncwarp();
+    } else if (warp >= 4 && warp < 8) {
+        // ------------------------------------------------ epilogue
+        const int ew = warp - 4;
+        uint8_t *stg_warp = epi + ew * 4096;
         uint32_t lt = 0;
+        int ebuf = 0;
         for (int tile = blockIdx.x; tile < p.total && ok; tile += gridDim.x, lt++) {
-            const int row = tile / p.ntn, n0 = (tile % p.ntn) * BN;
-            asm volatile("bar.sync 1, 128;" ::: "memory");   // the previous tile's table readers are done
-            for (int jj = et; jj < BN; jj += 128) {
-                const int n = min(n0 + jj, p.kn - 1);
-                sc_tab[jj] = p.scale ? __ldg(p.scale + n) : 1.0f;
-                sh_tab[jj] = p.shift ? __ldg(p.shift + n) : 0.0f;
-            }
+            const int row = tile / p.nwc, wc = tile % p.nwc;
             const int buf = lt & 1;
-            const bool mine = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 43);
-            // tables written, and every epilogue thread agrees whether to go on
-            uint32_t all_ok;
-            asm volatile(
-                "{\n\t.reg .pred pi, po;\n\tsetp.ne.u32 pi, %1, 0;\n\t"
-                "bar.red.and.pred po, 1, 128, pi;\n\tselp.u32 %0, 1, 0, po;\n\t}"
-                : "=r"(all_ok)
-                : "r"((uint32_t) mine)
-                : "memory");
-            if (!(ok = all_ok != 0)) break;
+            if (!(ok = tc::mbar_wait(&acc_full[buf], (lt >> 1) & 1, p.err, 43))) break;
             tc::tc_fence_after();
-            __nv_bfloat16 *orow = p.out + ((size_t) row * p.Wo + r) * p.kn;
             for (int c0 = 0; c0 < BN; c0 += 64) {
                 uint32_t v0[32], v1[32];
                 const uint32_t ta = tmem + ((uint32_t) (ew * 32) << 16) + (uint32_t) (buf * BN + c0);
@@ -204,51 +219,52 @@ __global__ void __launch_bounds__(288, 1)
                     tc::epi_bf16_64<true>(v0, v1, sc_tab + c0, sh_tab + c0, pk);
                 else
                     tc::epi_bf16_64<false>(v0, v1, sc_tab + c0, sh_tab + c0, pk);
-                const int nb = n0 + c0;
-                if (r >= p.Wo || nb >= p.kn) continue;
-                if (nb + 64 <= p.kn) {
-                    uint4 *dst = reinterpret_cast<uint4 *>(orow + nb);
+                if (lane == 0) bulk_wait_read<1>();   // the store that last read this staging buffer
+                __syncwarp();
+                uint8_t *stg = stg_warp + ebuf * STEM_EPI;
 #pragma unroll
-                    for (int q = 0; q < 8; q++) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
-                } else {
-                    uint32_t *dst = reinterpret_cast<uint32_t *>(orow + nb);
-#pragma unroll
-                    for (int q = 0; q < 32; q++)
-                        if (2 * q < p.kn - nb) dst[q] = pk[q];
+                for (int q = 0; q < 8; q++) {
+                    const uint4 u = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+                    *reinterpret_cast<uint4 *>(stg + lane * 128 + ((q ^ (lane & 7)) << 4)) = u;
                 }
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                const int ox0 = 128 * wc + ew * 32;
+                if (lane == 0 && ox0 < p.Wo && c0 < p.kn) tma_store_3d(&omap, tc::smem_u32(stg), c0, ox0, row);
+                ebuf ^= 1;
             }
         }
-    } else {
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    } else if (warp == 8) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 0, 0);
-            uint32_t it = 0, lt = 0;
-            ok = tc::mbar_wait(wfull, 0, p.err, 47);
-            for (int tile = blockIdx.x; tile < p.total && ok; tile += gridDim.x, lt++) {
-                const int buf = lt & 1;
-                if (lt >= 2) {
-                    ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) - 1) & 1, p.err, 44);
-                    if (!ok) break;
-                    tc::tc_fence_after();
-                }
-                const uint32_t dt = tmem + (uint32_t) (buf * BN);
-                for (int j0 = 0; j0 < p.ktiles; j0 += STEM_KB, it++) {
-                    const int s = it % STEM_STAGES;
-                    if (!tc::mbar_wait(&full[s], (it / STEM_STAGES) & 1, p.err, 45)) {
-                        ok = false;
-                        break;
-                    }
-                    tc::tc_fence_after();
-                    for (int kb = 0; kb < STEM_KB && j0 + kb < p.ktiles; kb++) {
-                        const uint32_t a0 = tc::smem_u32(base + s * C::STAGE + kb * STEM_A);
-                        const uint32_t b0 = tc::smem_u32(wres + (j0 + kb) * C::B_BYTES);
+            const uint32_t wbase = tc::smem_u32(wres);
+            // the low descriptor words of every pair's A operand (start within a slab buffer,
+            // lead) in registers: table loads between the MMAs would queue behind the TMA and
+            // tensor-core shared-memory traffic
+            uint32_t alo[STEM_MAXPAIRS];
 #pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            tc::mma_f16(dt, tc::sw128_desc(a0 + k * 32, 16, 1024),
-                                        tc::sw128_desc(b0 + k * 32, 16, 1024), idesc, (j0 | kb | k) != 0);
-                    }
-                    tc::mma_commit(&empty[s]);
+            for (int q = 0; q < STEM_MAXPAIRS; q++)
+                alo[q] = q < p.npairs ? (uint32_t) kmajor_desc(aoff_tab[q], alead_tab[q]) : 0u;
+            const uint64_t dhi = kmajor_desc(0, 0) & 0xFFFFFFFF00000000ull;   // SBO, version, layout
+            uint32_t lt = 0;
+            for (int tile = blockIdx.x; tile < p.total && ok; tile += gridDim.x, lt++) {
+                const int sb = lt & 1, buf = lt & 1;
+                if (lt >= 2) {
+                    if (!(ok = tc::mbar_wait(&acc_empty[buf], ((lt >> 1) + 1) & 1, p.err, 44))) break;
+                    tc::tc_fence_after();
                 }
+                if (!(ok = tc::mbar_wait(&slab_full[sb], (lt >> 1) & 1, p.err, 45))) break;
+                tc::tc_fence_after();
+                const uint32_t a0 = tc::smem_u32(slab + sb * p.buf_bytes);
+                const uint32_t dt = tmem + (uint32_t) (buf * BN);
+#pragma unroll
+                for (int q = 0; q < STEM_MAXPAIRS; q++)
+                    if (q < p.npairs)
+                        tc::mma_f16(dt, dhi | (uint64_t) (alo[q] + ((a0 & 0x3FFFF) >> 4)),
+                                    kmajor_desc(wbase + q * C::PAIR_W, BN * 16), idesc, q > 0);
+                tc::mma_commit(&slab_free[sb]);
                 tc::mma_commit(&acc_full[buf]);
             }
         }
@@ -261,7 +277,7 @@ __global__ void __launch_bounds__(288, 1)
 }
 
 template <int BN>
-cudaError_t launch_stem(const StemParams &p, const CUtensorMap &x, const CUtensorMap &w, int grid, cudaStream_t st) {
+cudaError_t launch_stem(const StemParams &p, const CUtensorMap &x, const CUtensorMap &o, int grid, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(tc_stem_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -269,28 +285,57 @@ cudaError_t launch_stem(const StemParams &p, const CUtensorMap &x, const CUtenso
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    return cg_launch_pdl(tc_stem_kernel<BN>, dim3(grid), dim3(288), StemCfg<BN>::SMEM, st, p, x, w);
+    return cg_launch_pdl(tc_stem_kernel<BN>, dim3(grid), dim3(288), StemCfg<BN>::SMEM, st, p, x, o);
+}
+
+int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+// The slab geometry of a shape; false when the path does not apply.
+struct StemGeom {
+    int bn, wc, qmin, qmax, nj, hbox, npairs;
+    uint32_t rho_bytes, buf_bytes;
+};
+
+bool stem_geom(const cg_shape &s, StemGeom &sg) {
+    // kn >= 64: the output store box is 64 channels wide
+    if (s.c > 8 || s.kn % 8 || s.kn < 64 || s.kn > 128 || s.kh * s.kw > STEM_MAXTAPS || s.hstride > 8) return false;
+    const ConvGeom g = make_geom(s);
+    if ((long long) s.b * g.ho * g.wo >= (1LL << 31)) return false;
+    sg.bn = s.kn > 64 ? 128 : 64;
+    sg.qmin = 1 << 30;
+    sg.qmax = -(1 << 30);
+    for (int kx = 0; kx < s.kw; kx++) {
+        const int q = floor_div(kx * s.hdil - s.hpad, s.hstride);
+        sg.qmin = std::min(sg.qmin, q);
+        sg.qmax = std::max(sg.qmax, q);
+    }
+    sg.wc = std::min(g.wo, 128);
+    sg.nj = sg.wc + sg.qmax - sg.qmin;
+    sg.hbox = (s.kh - 1) * s.vdil + 1;
+    sg.npairs = (s.kh * s.kw + 1) / 2;
+    sg.rho_bytes = (uint32_t) ((sg.hbox * sg.nj * 16 + 1023) / 1024 * 1024);
+    sg.buf_bytes = (uint32_t) s.hstride * sg.rho_bytes + STEM_ZERO;
+    return sg.nj * s.hstride <= 256 && sg.hbox <= 256 && (uint32_t) s.hstride * sg.rho_bytes <= STEM_SLAB_MAX &&
+           (uint32_t) sg.npairs * 2 * sg.bn * 16 <= STEM_W_MAX;
 }
 
 }  // namespace
 
 bool tc_stem_applicable(const cg_shape &s) {
-    const ConvGeom g = make_geom(s);
-    const long long wbox = (long long) (g.wo - 1) * s.hstride + (long long) (s.kw - 1) * s.hdil + 1;
-    const long long hbox = (long long) (s.kh - 1) * s.vdil + 1;
-    const int bn = s.kn > 64 ? 128 : 64;
-    const long long wbytes = (long long) ((s.kh * s.kw + 7) / 8) * bn * 128;
-    return s.c <= 8 && g.wo <= 128 && s.kh * s.kw <= STEM_MAXTAPS && s.kn % 8 == 0 && s.kn <= 128 &&
-           wbytes <= STEM_W_MAX && wbox <= 256 && hbox <= 256 && hbox * wbox * 16 <= STEM_SLAB_MAX &&
-           (long long) s.b * g.ho * g.wo < (1LL << 31);
+    StemGeom sg;
+    return stem_geom(s, sg);
 }
 
 convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,
                               const float *scale, const float *shift, int relu, cudaStream_t st) {
+    StemGeom sg;
+    if (!stem_geom(s, sg)) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "small-channel forward: shape");
     const ConvGeom g = make_geom(s);
+    const int ntaps = s.kh * s.kw;
+    if (((ntaps + 7) / 8) * 64 > Kpad) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "small-channel forward: packed K");
     StemParams p;
     memset(&p, 0, sizeof(p));
-    p.out = (__nv_bfloat16 *) y;
+    p.w = (const __nv_bfloat16 *) wpacked;
     p.scale = scale;
     p.shift = shift;
     p.relu = relu;
@@ -298,28 +343,66 @@ convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpac
     p.Ho = g.ho;
     p.Wo = g.wo;
     p.kn = s.kn;
-    p.ntaps = s.kh * s.kw;
-    p.ktiles = (p.ntaps + 7) / 8;
-    const int bn = s.kn > 64 ? 128 : 64;
-    p.ntn = (s.kn + bn - 1) / bn;
-    p.total = s.b * g.ho * p.ntn;
-    p.sw = s.hstride;
+    p.Kpad = Kpad;
+    p.nwc = (g.wo + 127) / 128;
+    p.total = s.b * g.ho * p.nwc;
     p.sh = s.vstride;
+    p.sw = s.hstride;
     p.pad_h = s.vpad;
-    p.pad_w = s.hpad;
-    p.Wbox = (g.wo - 1) * s.hstride + (s.kw - 1) * s.hdil + 1;
-    p.Hbox = (s.kh - 1) * s.vdil + 1;
+    p.qmin = sg.qmin;
+    p.npairs = sg.npairs;
+    p.rho_bytes = sg.rho_bytes;
+    p.buf_bytes = sg.buf_bytes;
+    p.slab_tx = (uint32_t) s.hstride * sg.hbox * sg.nj * 16;
     p.err = cg_device_error_word();
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
-    if (p.ktiles * 64 > Kpad) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "small-channel forward: packed K");
-    for (int kx = 0; kx < s.kh; kx++)
-        for (int ky = 0; ky < s.kw; ky++) p.tapoff[kx * s.kw + ky] = kx * s.vdil * p.Wbox + ky * s.hdil;
-    CUtensorMap xmap, wmap;
-    if (convgemm_status_t e = tc_make_map_4d_box(&xmap, x, s.b, s.h, s.w, 8, p.Hbox, p.Wbox)) return e;
-    if (convgemm_status_t e = tc_make_map_2d(&wmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, wpacked, s.kn, Kpad, 64, bn))
-        return e;
+    // every tap's rows in a slab buffer, sorted by address and paired
+    struct TapAt {
+        uint32_t off;
+        int tap;
+    } taps[STEM_MAXTAPS];
+    for (int ky = 0; ky < s.kh; ky++)
+        for (int kx = 0; kx < s.kw; kx++) {
+            const int off = kx * s.hdil - s.hpad;
+            const int q = floor_div(off, s.hstride), rho = off - q * s.hstride;
+            taps[ky * s.kw + kx] = {(uint32_t) rho * sg.rho_bytes + (uint32_t) (ky * s.vdil * sg.nj + q - sg.qmin) * 16,
+                                    ky * s.kw + kx};
+        }
+    std::sort(taps, taps + ntaps, [](const TapAt &a, const TapAt &b) { return a.off < b.off; });
+    const uint32_t zero_off = (uint32_t) s.hstride * sg.rho_bytes;
+    for (int q = 0; q < sg.npairs; q++) {
+        const TapAt &t1 = taps[2 * q];
+        p.aoff[q] = t1.off;
+        p.wtap[2 * q] = (int16_t) t1.tap;
+        if (2 * q + 1 < ntaps) {
+            p.alead[q] = taps[2 * q + 1].off - t1.off;
+            p.wtap[2 * q + 1] = (int16_t) taps[2 * q + 1].tap;
+        } else {
+            p.alead[q] = zero_off - t1.off;
+            p.wtap[2 * q + 1] = -1;
+        }
+    }
+    // input [B][H][W][8]: box {8, nj * sw (traversal stride sw: nj pixels), hbox rows, 1 image}
+    CUtensorMap xmap, omap;
+    {
+        const unsigned long long dims[4] = {8, (unsigned long long) s.w, (unsigned long long) s.h,
+                                            (unsigned long long) s.b};
+        const unsigned long long str[3] = {16, 16ull * s.w, 16ull * s.w * s.h};
+        const unsigned box[4] = {8, (unsigned) (sg.nj * s.hstride), (unsigned) sg.hbox, 1};
+        const unsigned estr[4] = {1, (unsigned) s.hstride, 1, 1};
+        if (convgemm_status_t e = tc_make_map_nd(&xmap, 4, x, dims, str, box, estr, 0)) return e;
+    }
+    // output [B*Ho][Wo][kn]: box {64 channels, 32 pixels, 1 row}, 128-byte swizzle
+    {
+        const unsigned long long dims[3] = {(unsigned long long) s.kn, (unsigned long long) g.wo,
+                                            (unsigned long long) s.b * g.ho};
+        const unsigned long long str[2] = {2ull * s.kn, 2ull * s.kn * g.wo};
+        const unsigned box[3] = {64, 32, 1};
+        const unsigned estr[3] = {1, 1, 1};
+        if (convgemm_status_t e = tc_make_map_nd(&omap, 3, y, dims, str, box, estr, 1)) return e;
+    }
     const int sms = tc_num_sms();
     const int grid = p.total < sms ? p.total : sms;
-    return cg_cuda_check(bn == 64 ? launch_stem<64>(p, xmap, wmap, grid, st) : launch_stem<128>(p, xmap, wmap, grid, st),
+    return cg_cuda_check(sg.bn == 64 ? launch_stem<64>(p, xmap, omap, grid, st) : launch_stem<128>(p, xmap, omap, grid, st),
                          "small-channel forward launch");
 }

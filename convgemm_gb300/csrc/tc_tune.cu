@@ -35,10 +35,14 @@ extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *s
     if (bn != 0 && bn != 64 && bn != 128 && bn != 256)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: tile width %d is not 0/64/128/256", bn);
     const bool mt_op = op == CONVGEMM_TUNE_FWD || op == CONVGEMM_TUNE_DGRAD;
-    if (splits < 0 || (op != CONVGEMM_TUNE_WGRAD && splits > (mt_op ? 2 : 0)))
+    // forward / input gradient: M tiles per weight tile (1 / 2) + 4 for eight epilogue warps
+    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? splits >= 0
+                        : mt_op ? (splits == 0 || splits == 1 || splits == 2 || splits == 5 || splits == 6)
+                                : splits == 0;
+    if (!aux_ok)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE,
-                            "convgemm_tune_set: aux is the weight gradient's split count, or 1/2 M tiles per weight "
-                            "tile of the BF16 forward / input gradient");
+                            "convgemm_tune_set: aux is the weight gradient's split count, or for the BF16 forward / "
+                            "input gradient 1 / 2 M tiles per weight tile, plus 4 for eight epilogue warps");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     if (bn == 0 && splits == 0)
         g_tune.erase(key_of(op, *shape));

@@ -222,7 +222,8 @@ enum {
  * shape, as chosen by an autotuner: bn = output channels per tile (64, 128 or
  * 256; for the weight gradient the width of its N side); aux = pixel splits of
  * the weight gradient, or, for the BF16 forward / input gradient, the number of
- * 128-row M tiles (1 or 2) that share each weight tile (0 = heuristic).
+ * 128-row M tiles (1 or 2) that share each weight tile, plus 4 for the kernel
+ * form with eight epilogue warps (short-K layers; 0 = heuristic).
  * bn = aux = 0 removes the entry.  Set the weight-gradient entry before querying
  * its workspace size.  Thread-safe. */
 convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int aux);

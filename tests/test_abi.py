@@ -104,6 +104,9 @@ def test_tune_table_validation_without_gpu(cglib):
     assert L.convgemm_tune_set(9, ctypes.byref(s), 64, 0) == 1
     assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 96, 0) == 1
     assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 64, 4) == 1      # splits: weight gradient only
+    assert L.convgemm_tune_set(tc.TUNE_FWD, ctypes.byref(s), 64, 3) == 1
+    assert L.convgemm_tune_set(tc.TUNE_DGRAD, ctypes.byref(s), 128, 6) == 0    # 2 M tiles, 8 epilogue warps
+    assert L.convgemm_tune_set(tc.TUNE_FWD_FP8, ctypes.byref(s), 128, 1) == 1
     assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 0, 3) == 0
     tc.tune_clear()
 

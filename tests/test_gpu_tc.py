@@ -207,7 +207,10 @@ def test_tuned_tile_configurations_agree(cglib, oracle_lib):
     wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
     try:
         ys, dxs = [], []
-        for bn, mt in ((64, 1), (128, 1), (256, 1), (64, 2), (128, 2), (256, 2)):
+        # aux + 4: the kernel form with eight epilogue warps ((64, 5) is not a valid pairing and
+        # falls back to four)
+        for bn, mt in ((64, 1), (128, 1), (256, 1), (64, 2), (128, 2), (256, 2), (128, 5), (256, 5), (64, 6),
+                       (128, 6), (64, 5)):
             tc.tune_set(tc.TUNE_FWD, s, bn, mt)
             tc.tune_set(tc.TUNE_DGRAD, s, bn, mt)
             y = torch.empty(b, h, w, kn, dtype=torch.bfloat16, device="cuda")
@@ -292,7 +295,7 @@ def test_two_m_tiles_strided_input_gradient(cglib, oracle_lib):
     wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
     try:
         outs = []
-        for mt in (1, 2):
+        for mt in (1, 2, 5, 6):
             tc.tune_set(tc.TUNE_DGRAD, s, 128, mt)
             tc.tune_set(tc.TUNE_FWD, s, 128, mt)
             dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
@@ -302,7 +305,8 @@ def test_two_m_tiles_strided_input_gradient(cglib, oracle_lib):
             outs.append((dx, y))
         torch.cuda.synchronize()
         cg.check_device()
-        assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+        for o in outs[1:]:
+            assert torch.equal(outs[0][0], o[0]) and torch.equal(outs[0][1], o[1])
         ref = O.dgrad_f64(C.NHWC, g, wt, dy)
         assert rel_max_rms(outs[1][0].float().cpu().numpy(), ref)[0] <= BF16_TOL
     finally:
