@@ -210,7 +210,7 @@ __global__ void pack_split_kernel(const float *__restrict__ w, int nchw, int C, 
 // search costs one global round trip.
 __global__ void __launch_bounds__(256) prep_group_kernel(const PrepJob *__restrict__ jobs, const int *__restrict__ b0,
                                                          int njobs) {
-    __shared__ float tile[32][33];
+    __shared__ float tile[64][65];
     extern __shared__ int s_b0[];
     tc::pdl_wait();
     tc::pdl_trigger();
@@ -239,23 +239,56 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const PrepJob *__restri
             return;
         }
         case PREP_FWD_TILED: {
-            // the tiled transpose of pack_fwd_tiled_kernel for one (ci tile, co tile), all taps
-            const int nci = (J.Cp + 31) / 32;
-            const int ci0 = (lb % nci) * 32, co0 = (lb / nci) * 32;
-            const int tx = t & 31, ty = t >> 5, khw = J.kh * J.kw;
+            // NHWC-API weights [ci][tap][co] -> out[co][tap*Cp + ci]: one block per (tap, 64 ci x 64 co
+            // tile); four independent 16-byte loads per thread along co, a padded shared-memory
+            // transpose, 8-byte stores of four BF16 along ci
+            const int nci = (J.Cp + 63) / 64, nco = (J.kn + 63) / 64, khw = J.kh * J.kw;
+            const int tap = lb / (nci * nco), rem = lb % (nci * nco);
+            const int ci0 = (rem % nci) * 64, co0 = (rem / nci) * 64;
+            const int cq = (t & 15) * 4, r0 = t >> 4;   // 4 co per thread; rows r0 + 16 i
+            const bool vec_in = ((J.kn & 3) == 0) && (((uintptr_t) J.w & 15) == 0);
+            const bool vec_out = ((J.Kpad & 3) == 0) && ((J.Cp & 3) == 0) && (((uintptr_t) J.out & 7) == 0);
+            float4 v[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int ci = ci0 + r0 + 16 * i, co = co0 + cq;
+                const float *src = J.w + ((size_t) ci * khw + tap) * J.kn + co;
+                if (ci < J.C && co + 4 <= J.kn && vec_in) {
+                    v[i] = __ldg(reinterpret_cast<const float4 *>(src));
+                } else {
+                    float e[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) e[q] = (ci < J.C && co + q < J.kn) ? __ldg(src + q) : 0.0f;
+                    v[i] = make_float4(e[0], e[1], e[2], e[3]);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                float *d = &tile[r0 + 16 * i][cq];
+                d[0] = v[i].x;
+                d[1] = v[i].y;
+                d[2] = v[i].z;
+                d[3] = v[i].w;
+            }
+            __syncthreads();
             bf16 *out = (bf16 *) J.out;
-            for (int tap = 0; tap < khw; tap++) {
-                for (int i = ty; i < 32; i += 8) {
-                    const int ci = ci0 + i, co = co0 + tx;
-                    tile[i][tx] = (ci < J.C && co < J.kn) ? J.w[((size_t) ci * khw + tap) * J.kn + co] : 0.0f;
+            const int cw = (t & 15) * 4, o0 = t >> 4;   // 4 ci per thread; co rows o0 + 16 j
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int co = co0 + o0 + 16 * j, ci = ci0 + cw;
+                if (co >= J.kn || ci >= J.Cp) continue;
+                bf16 *dst = out + (size_t) co * J.Kpad + (size_t) tap * J.Cp + ci;
+                const int cc = o0 + 16 * j;
+                if (ci + 4 <= J.Cp && vec_out) {
+                    __nv_bfloat162 lo = __floats2bfloat162_rn(tile[cw][cc], tile[cw + 1][cc]);
+                    __nv_bfloat162 hi = __floats2bfloat162_rn(tile[cw + 2][cc], tile[cw + 3][cc]);
+                    uint2 u;
+                    u.x = *reinterpret_cast<uint32_t *>(&lo);
+                    u.y = *reinterpret_cast<uint32_t *>(&hi);
+                    *reinterpret_cast<uint2 *>(dst) = u;
+                } else {
+                    for (int q = 0; q < 4 && ci + q < J.Cp; q++) dst[q] = __float2bfloat16_rn(tile[cw + q][cc]);
                 }
-                __syncthreads();
-                for (int j = ty; j < 32; j += 8) {
-                    const int co = co0 + j, ci = ci0 + tx;
-                    if (co < J.kn && ci < J.Cp)
-                        out[(size_t) co * J.Kpad + (size_t) tap * J.Cp + ci] = __float2bfloat16_rn(tile[tx][j]);
-                }
-                __syncthreads();
             }
             return;
         }
@@ -283,6 +316,33 @@ __global__ void __launch_bounds__(256) prep_group_kernel(const PrepJob *__restri
             const int c = lb % J.info.ncls, ci0 = (lb / J.info.ncls) * 4;
             const int beg = J.info.kbeg[c], end = c + 1 < J.info.ncls ? J.info.kbeg[c + 1] : J.info.Ktot;
             const int nt = J.info.ntaps[c];
+            if (!J.nchw && (J.kn & 3) == 0 && (J.knp & 3) == 0 && ((beg | end | J.info.Ktot) & 3) == 0 &&
+                ((uintptr_t) J.w & 15) == 0 && ((uintptr_t) J.out & 7) == 0) {
+                // NHWC-API weights: four consecutive output channels per 16-byte load and 8-byte
+                // store, unrolled for several loads in flight
+                const int nq = (end - beg) >> 2;
+                for (int r = 0; r < 4; r++) {
+                    const int ci = ci0 + r;
+                    if (ci >= J.C) break;
+                    bf16 *row = (bf16 *) J.out + (size_t) ci * J.info.Ktot + beg;
+#pragma unroll 4
+                    for (int q = t; q < nq; q += 256) {
+                        const int idx = q * 4;
+                        const int g = (int) J.dknp.div((uint32_t) idx), co = idx - g * J.knp;
+                        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        if (g < nt && co < J.kn) {
+                            const int tap = J.info.kx[c][g] * J.kw + J.info.ky[c][g];
+                            v = __ldg(reinterpret_cast<const float4 *>(J.w + ((size_t) ci * J.kh * J.kw + tap) * J.kn + co));
+                        }
+                        __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+                        uint2 u;
+                        u.x = *reinterpret_cast<uint32_t *>(&lo);
+                        u.y = *reinterpret_cast<uint32_t *>(&hi);
+                        *reinterpret_cast<uint2 *>(row + idx) = u;
+                    }
+                }
+                return;
+            }
             for (int r = 0; r < 4; r++) {
                 const int ci = ci0 + r;
                 if (ci >= J.C) break;
@@ -377,5 +437,12 @@ cudaError_t prep_pack_split(const float *w, int nchw, int C, int kh, int kw, int
 
 cudaError_t prep_group_launch(const PrepJob *jobs, int njobs, int nblocks, cudaStream_t st) {
     const int *b0 = (const int *) (jobs + njobs);
+    static bool attr = false;   // up to 12288 job offsets (48 KB) beside the 16.6 KB transpose tile
+    if (!attr) {
+        if (cudaError_t e = cudaFuncSetAttribute(prep_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 12288 * (int) sizeof(int)))
+            return e;
+        attr = true;
+    }
     return cg_launch_pdl(prep_group_kernel, dim3(nblocks), dim3(256), sizeof(int) * njobs, st, jobs, b0, njobs);
 }

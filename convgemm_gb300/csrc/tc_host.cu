@@ -732,7 +732,7 @@ extern "C" convgemm_status_t convgemm_prep_prepare(int n, const convgemm_prep_it
                 add(f, (long long) s.kn * ((f.Kpad + 255) / 256));
             } else {
                 f.type = PREP_FWD_TILED;
-                add(f, (long long) ((f.Cp + 31) / 32) * ((s.kn + 31) / 32));
+                add(f, (long long) khw * ((f.Cp + 63) / 64) * ((s.kn + 63) / 64));
                 if (f.Kpad > khw * f.Cp) {
                     if ((long long) s.kn * (f.Kpad - khw * f.Cp) > (1LL << 31) - 256)
                         return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: item %d: weights too large", fn, i);

@@ -247,7 +247,9 @@ def test_grouped_preparation_matches_per_layer_calls(cglib):
     shapes = [(cg.NHWC, cg.Shape.of(2, 20, 20, 3, 64, 7, 7, 3, 3, 2, 2)),       # stem: K tail
               (cg.NHWC, cg.Shape.of(2, 14, 14, 128, 256, 3, 3, 1, 1, 2, 2)),    # stride-2 dgrad classes
               (cg.NCHW, cg.Shape.of(2, 9, 9, 40, 72, 3, 3, 1, 1, 1, 1)),        # NCHW, ragged
-              (cg.NHWC, cg.Shape.of(2, 8, 8, 256, 64, 1, 1))]
+              (cg.NHWC, cg.Shape.of(2, 8, 8, 256, 64, 1, 1)),
+              (cg.NHWC, cg.Shape.of(2, 9, 9, 40, 72, 3, 3, 1, 1, 2, 2)),       # partial 64 x 64 tiles
+              (cg.NHWC, cg.Shape.of(1, 6, 6, 16, 6, 3, 3, 1, 1))]              # kn % 4 != 0: scalar paths
     items, ref = [], []
     for li, (layout, s) in enumerate(shapes):
         K = s.c * s.kh * s.kw
