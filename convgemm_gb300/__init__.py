@@ -123,6 +123,12 @@ def lib():
         L.convgemm_bias_grad_bf16_workspace_size.argtypes = [SP]
         L.convgemm_bias_grad_bf16_workspace_size.restype = ctypes.c_size_t
         L.convgemm_bias_grad_bf16.argtypes = [SP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
+        L.convgemm_fwd_bf16_stats_workspace_size.argtypes = [SP]
+        L.convgemm_fwd_bf16_stats_workspace_size.restype = ctypes.c_size_t
+        L.convgemm_fwd_bf16_stats.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _I, _VP, _VP, ctypes.c_size_t, _VP]
+        L.convgemm_bn_stats_fold.argtypes = [_I, _VP, ctypes.c_longlong, _VP, _VP, ctypes.c_float, _VP, _VP, _VP,
+                                             _VP, _VP]
+        L.convgemm_bn_apply_bf16.argtypes = [ctypes.c_longlong, _I, _VP, _VP, _VP, _I, _VP, _VP]
         _HG = [_I] * 14
         L.im2row_nhwc.argtypes = [_VP, _I, _VP] + _HG
         L.im2col_nchw.argtypes = [_VP, _I, _VP] + _HG

@@ -139,7 +139,7 @@ __device__ __forceinline__ Tile decode_tile(const ClsS *cls, int ncls, int ntile
     return tl;
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT, int EW>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT, int EW, bool STATS>
 __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     tc_conv_kernel(const __grid_constant__ TcConvParams p, const __grid_constant__ CUtensorMap wmap,
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
@@ -395,6 +395,21 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
                 const int nb = tl.n0 + c0;
+                if constexpr (STATS) if (m0 + ew * 32 < M) {
+                    // batch-norm statistics of this chunk's 64 columns over the warp's 32 rows
+                    // (group (m0 + 32 ew) / 32 of the ceil(M / 32) the workspace holds)
+                    float *part = p.stats + (size_t) ((m0 >> 5) + ew) * 2 * p.Cout;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        float sum, sq;
+                        tc::stats_cols32(h ? v1 : v0, scp + c0 + 32 * h, shp + c0 + 32 * h, m < M, sum, sq);
+                        const int col = nb + 32 * h + lane;
+                        if (col < p.Cout) {
+                            part[col] = sum;
+                            part[p.Cout + col] = sq;
+                        }
+                    }
+                }
                 uint32_t pk[32];   // one 128-byte output row chunk
                 if (C::OUTF32) {
 #pragma unroll
@@ -545,11 +560,12 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     if (warp == C::MMA_WARP) tc::tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
-template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT = 1, int EW = 4>
+template <int BN, int STAGES, int KB, bool IM2C, int MODE, int MT = 1, int EW = 4, bool STATS = false>
 cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap, const TcMaps &amaps,
                       int grid, cudaStream_t st) {
+    static_assert(!STATS || (MODE == MODE_BF16 && MT == 1 && EW == 4), "statistics: BF16, one M tile, four warps");
     using C = TcCfg<BN, STAGES, KB, MODE, MT, EW>;
-    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE, MT, EW>;
+    auto kern = tc_conv_kernel<BN, STAGES, KB, IM2C, MODE, MT, EW, STATS>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -580,6 +596,24 @@ cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const
             case 64: return launch_bn<64, 4, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
             case 128: return launch_bn<128, 3, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
             case 256: return launch_bn<256, 2, 1, true, MODE_X3>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (p.stats) {
+        // forward with batch statistics (tc_conv_kernel's STATS form): one M tile, four epilogue warps
+        if (p.mode != MODE_BF16 || p.mt != 1 || p.ew != 4) return cudaErrorInvalidValue;
+        if (p.im2col) {
+            switch (p.bn) {
+                case 64: return launch_bn<64, 4, 2, true, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
+                case 128: return launch_bn<128, 3, 2, true, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
+                case 256: return launch_bn<256, 3, 1, true, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        switch (p.bn) {
+            case 64: return launch_bn<64, 8, 1, false, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 6, 1, false, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 4, 1, false, MODE_BF16, 1, 4, true>(p, wmap, omap, amaps, grid, st);
             default: return cudaErrorInvalidValue;
         }
     }

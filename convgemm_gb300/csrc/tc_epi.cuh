@@ -42,4 +42,44 @@ __device__ __forceinline__ void epi_bf16_64(const uint32_t (&v0)[32], const uint
     }
 }
 
+// One transpose-reduction round over the warp: lanes with bit `O` set keep the upper
+// half of x[0..S), the others the lower half; each adds the half its partner lane O
+// away kept for it.  After the rounds O = 16, 8, 4, 2, 1 lane l holds column l.
+template <int S, int O>
+__device__ __forceinline__ void stats_round(float (&x)[16], float (&y)[16], int lane) {
+    const bool up = (lane & O) != 0;
+#pragma unroll
+    for (int i = 0; i < S / 2; i++) {
+        const float kx = up ? x[i + S / 2] : x[i], sx = up ? x[i] : x[i + S / 2];
+        const float ky = up ? y[i + S / 2] : y[i], sy = up ? y[i] : y[i + S / 2];
+        x[i] = kx + __shfl_xor_sync(0xFFFFFFFFu, sx, O);
+        y[i] = ky + __shfl_xor_sync(0xFFFFFFFFu, sy, O);
+    }
+}
+
+// Batch statistics of 32 accumulator columns of the warp's 32 rows (one row per
+// lane): z = acc * scale + shift (FP32, before ReLU and rounding; 0 for rows outside
+// the output), summed over the 32 rows.  Lane l returns the sum and the sum of
+// squares of column l.
+__device__ __forceinline__ void stats_cols32(const uint32_t (&v)[32], const float *__restrict__ sc,
+                                             const float *__restrict__ sh, bool valid, float &sum, float &sq) {
+    const int lane = threadIdx.x & 31;
+    float x[16], y[16];
+    const bool up = (lane & 16) != 0;
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        const float za = valid ? fmaf(__uint_as_float(v[i]), sc[i], sh[i]) : 0.0f;
+        const float zb = valid ? fmaf(__uint_as_float(v[i + 16]), sc[i + 16], sh[i + 16]) : 0.0f;
+        const float kz = up ? zb : za, sz = up ? za : zb;
+        x[i] = kz + __shfl_xor_sync(0xFFFFFFFFu, sz, 16);
+        y[i] = kz * kz + __shfl_xor_sync(0xFFFFFFFFu, sz * sz, 16);
+    }
+    stats_round<16, 8>(x, y, lane);
+    stats_round<8, 4>(x, y, lane);
+    stats_round<4, 2>(x, y, lane);
+    stats_round<2, 1>(x, y, lane);
+    sum = x[0];
+    sq = y[0];
+}
+
 }  // namespace tc

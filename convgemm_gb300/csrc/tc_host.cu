@@ -302,7 +302,7 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
                          const void *in_lo, const void *w_lo, int bn_override, int aux_override,
-                         const void *mask) {
+                         const void *mask, float *stats) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     const int sms = tc_num_sms();
     TcConvParams p;
@@ -333,6 +333,7 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     p.shift = shift;
     p.relu = relu;
     p.mask = (const __nv_bfloat16 *) mask;
+    p.stats = stats;
     p.B = s.b;
     p.Hin = pl.Hin;
     p.Win = pl.Win;
@@ -382,6 +383,10 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
         ew8 = kmax <= 8;
     }
     p.ew = (ew8 && mode == 0 && p.im2col && (p.bn >= 128 || p.mt == 2) && !(p.bn == 256 && p.mt == 2)) ? 8 : 4;
+    if (stats) {   // the statistics form: one M tile, four epilogue warps
+        p.mt = 1;
+        p.ew = 4;
+    }
     int t0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
         p.cls[c] = pi.cls[c];

@@ -34,7 +34,10 @@ convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, co
 // Forward of convolutions with at most 8 input channels (tc_stem.cu).
 bool tc_stem_applicable(const cg_shape &s);
 convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,
-                              const float *scale, const float *shift, int relu, cudaStream_t st);
+                              const float *scale, const float *shift, int relu, cudaStream_t st,
+                              float *stats = nullptr);
+// Statistics groups the small-channel forward writes: 4 per (image row, 128-pixel chunk).
+int tc_stem_stat_groups(const cg_shape &s);
 
 int tc_num_sms();
 // Autotuned tile configuration of one operation on one shape (0 = heuristic):
@@ -49,4 +52,5 @@ bool tc_tune_get(int op, const convgemm_shape_t &s, TcTune *t);
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,
                          const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0,
-                         int aux_override = 0, const void *mask = nullptr);
+                         int aux_override = 0, const void *mask = nullptr,
+                         float *stats = nullptr);

@@ -58,6 +58,7 @@ struct StemParams {
     uint32_t rho_bytes;       // one residue slab, 1024-aligned
     uint32_t slab_tx;         // bytes the TMA loads of one tile deliver
     int *err;
+    float *stats;             // per (tile, epilogue warp) group g: [g][0][kn] sum, [g][1][kn] sum of squares, or NULL
     uint32_t aoff[STEM_MAXPAIRS];   // byte offset of the pair's first tap rows within a slab buffer
     uint32_t alead[STEM_MAXPAIRS];  // bytes from the first to the second tap's rows (or to the zero region)
     int16_t wtap[2 * STEM_MAXPAIRS];   // the pair's taps (ky * kw + kx) in the packed weights; -1 = zero
@@ -214,6 +215,21 @@ __global__ void __launch_bounds__(288, 1)
                     tc::tc_fence_before();
                     tc::mbar_arrive(&acc_empty[buf]);
                 }
+                if (p.stats) {
+                    // batch-norm statistics of the 64 columns over this warp's 32 pixels
+                    float *part = p.stats + ((size_t) tile * 4 + ew) * 2 * p.kn;
+                    const bool valid = 128 * wc + ew * 32 + lane < p.Wo;
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        float sum, sq;
+                        tc::stats_cols32(h ? v1 : v0, sc_tab + c0 + 32 * h, sh_tab + c0 + 32 * h, valid, sum, sq);
+                        const int col = c0 + 32 * h + lane;
+                        if (col < p.kn) {
+                            part[col] = sum;
+                            part[p.kn + col] = sq;
+                        }
+                    }
+                }
                 uint32_t pk[32];
                 if (p.relu)
                     tc::epi_bf16_64<true>(v0, v1, sc_tab + c0, sh_tab + c0, pk);
@@ -326,8 +342,13 @@ bool tc_stem_applicable(const cg_shape &s) {
     return stem_geom(s, sg);
 }
 
+int tc_stem_stat_groups(const cg_shape &s) {
+    const ConvGeom g = make_geom(s);
+    return s.b * g.ho * ((g.wo + 127) / 128) * 4;
+}
+
 convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,
-                              const float *scale, const float *shift, int relu, cudaStream_t st) {
+                              const float *scale, const float *shift, int relu, cudaStream_t st, float *stats) {
     StemGeom sg;
     if (!stem_geom(s, sg)) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "small-channel forward: shape");
     const ConvGeom g = make_geom(s);
@@ -356,6 +377,7 @@ convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpac
     p.slab_tx = (uint32_t) s.hstride * sg.hbox * sg.nj * 16;
     p.err = cg_device_error_word();
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
+    p.stats = stats;
     // every tap's rows in a slab buffer, sorted by address and paired
     struct TapAt {
         uint32_t off;

@@ -60,6 +60,36 @@ def bias_grad_bf16(shape: Shape, dy, db, workspace=None, stream=None):
                                             workspace.numel() * workspace.element_size(), _stream(stream)))
 
 
+def fwd_bf16_stats_workspace_size(shape: Shape) -> int:
+    return lib().convgemm_fwd_bf16_stats_workspace_size(ctypes.byref(shape))
+
+
+def fwd_bf16_stats(shape: Shape, x, wpacked, y, stats, scale=None, shift=None, relu=False, workspace=None,
+                   stream=None):
+    """BF16 forward with the batch statistics of z = conv * scale + shift fused into the
+    epilogue: stats (FP64 [2][kn], device) = per-channel sums and sums of squares."""
+    import torch
+    n = fwd_bf16_stats_workspace_size(shape)
+    if workspace is None:
+        workspace = torch.empty(n // 8 + 2, dtype=torch.float64, device=x.device)
+    _raise_if(lib().convgemm_fwd_bf16_stats(ctypes.byref(shape), ptr(x), ptr(wpacked), ptr(y), ptr(scale),
+                                            ptr(shift), int(relu), ptr(stats), ptr(workspace),
+                                            workspace.numel() * workspace.element_size(), _stream(stream)))
+
+
+def bn_stats_fold(kn: int, stats, count: int, scale, shift, gamma=None, beta=None, eps: float = 1e-5,
+                  batch_mean=None, batch_var=None, stream=None):
+    """scale / shift of training-mode batch norm from the forward's batch statistics."""
+    _raise_if(lib().convgemm_bn_stats_fold(kn, ptr(stats), count, ptr(gamma), ptr(beta), eps, ptr(scale),
+                                           ptr(shift), ptr(batch_mean), ptr(batch_var), _stream(stream)))
+
+
+def bn_apply_bf16(npix: int, kn: int, z, scale, shift, y, relu=True, stream=None):
+    """y = relu?(z * scale + shift) per channel (BF16 NHWC)."""
+    _raise_if(lib().convgemm_bn_apply_bf16(npix, kn, ptr(z), ptr(scale), ptr(shift), int(relu), ptr(y),
+                                           _stream(stream)))
+
+
 def wgrad_bf16_workspace_size(shape: Shape) -> int:
     return lib().convgemm_wgrad_bf16_workspace_size(ctypes.byref(shape))
 

@@ -280,6 +280,29 @@ size_t convgemm_bias_grad_bf16_workspace_size(const convgemm_shape_t *shape);
 convgemm_status_t convgemm_bias_grad_bf16(const convgemm_shape_t *shape, const void *dy, float *db, void *workspace,
                                           size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------ training-mode batch normalisation
+ * The BF16 forward with batch statistics fused into its epilogue: y as
+ * convgemm_fwd_bf16, and stats (FP64, device) = [0][kn] the sums and [1][kn] the
+ * sums of squares over the b*ho*wo output pixels of z = conv * scale + shift (FP32,
+ * before ReLU and BF16 rounding).  Partial sums per 32 pixels go to the workspace
+ * and are reduced in a fixed order (bit-reproducible).  For a training step call it
+ * with relu = 0 and scale / shift = NULL (or a bias as shift), fold the statistics
+ * (convgemm_bn_stats_fold) and normalise (convgemm_bn_apply_bf16). */
+size_t convgemm_fwd_bf16_stats_workspace_size(const convgemm_shape_t *shape);
+convgemm_status_t convgemm_fwd_bf16_stats(const convgemm_shape_t *shape, const void *x, const void *wpacked, void *y,
+                                          const float *scale, const float *shift, int relu, double *stats,
+                                          void *workspace, size_t workspace_bytes, void *stream);
+/* scale = gamma / sqrt(var + eps), shift = beta - mean * scale from the batch mean
+ * = stats[0] / count and biased variance stats[1] / count - mean^2 (FP64); gamma /
+ * beta NULL = 1 / 0; batch_mean / batch_var (FP32, optional) receive mean and var. */
+convgemm_status_t convgemm_bn_stats_fold(int kn, const double *stats, long long count, const float *gamma,
+                                         const float *beta, float eps, float *scale, float *shift, float *batch_mean,
+                                         float *batch_var, void *stream);
+/* y = relu?(z * scale + shift) per channel, BF16 NHWC [npix][kn] (kn % 8 == 0;
+ * z == y allowed). */
+convgemm_status_t convgemm_bn_apply_bf16(long long npix, int kn, const void *z, const float *scale,
+                                         const float *shift, int relu, void *y, void *stream);
+
 /* Workspace of convgemm_wgrad_bf16 in bytes: FP32 partial tiles of the pixel splits. */
 size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape);
 

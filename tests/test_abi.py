@@ -125,3 +125,22 @@ def test_set_pdl_is_per_thread_and_restores_default(cglib, monkeypatch):
     assert cglib.set_pdl(1) == 0
     assert cglib.set_pdl(-1) == 1
     assert cglib.set_pdl(-1) == default
+
+
+def test_batch_norm_training_entry_points_validate_without_gpu(cglib):
+    """Workspace sizes of the statistics forward and argument checks of the fold / apply."""
+    L = cglib.lib()
+    s = cglib.Shape.of(2, 14, 14, 64, 128, 3, 3, 1, 1)
+    groups = -(-(2 * 14 * 14) // 32)
+    chunks = -(-groups // 256)
+    assert L.convgemm_fwd_bf16_stats_workspace_size(ctypes.byref(s)) == chunks * 2 * 128 * 8 + groups * 2 * 128 * 4
+    stem = cglib.Shape.of(2, 20, 20, 3, 64, 7, 7, 3, 3, 2, 2)       # small-channel kernel: 4 groups per row chunk
+    assert L.convgemm_fwd_bf16_stats_workspace_size(ctypes.byref(stem)) == 1 * 2 * 64 * 8 + 2 * 10 * 4 * 2 * 64 * 4
+    bad = cglib.Shape.of(0, 14, 14, 64, 128, 3, 3, 1, 1)
+    assert L.convgemm_fwd_bf16_stats_workspace_size(ctypes.byref(bad)) == 0
+    assert L.convgemm_fwd_bf16_stats(ctypes.byref(s), None, None, None, None, None, 0, None, None, 0, None) == 1
+    assert L.convgemm_fwd_bf16_stats(ctypes.byref(s), 16, 16, 16, None, None, 0, 16, 16, 8, None) != 0   # workspace
+    assert "workspace" in cglib.last_error()[1]
+    assert L.convgemm_bn_stats_fold(0, 16, 10, None, None, 1e-5, 16, 16, None, None, None) == 1
+    assert L.convgemm_bn_stats_fold(8, 16, 0, None, None, 1e-5, 16, 16, None, None, None) == 1
+    assert L.convgemm_bn_apply_bf16(10, 12, 16, 16, 16, 1, 16, None) == 1     # kn % 8
