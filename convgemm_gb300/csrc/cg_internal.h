@@ -50,13 +50,19 @@ cudaError_t cg_helper_col2im(const float *cols, float *out, int b, int c, int h,
 cudaError_t cg_helper_transpose(int rows, int cols, const float *in, int ld, float beta, float *out, int kn, int ho,
                                 int wo, int start_row, int start_col, cudaStream_t st);
 
-bool cg_pdl_enabled();
+bool cg_pdl_enabled();       // this host thread's setting (convgemm_set_pdl), default: the environment's
+bool cg_pdl_env_enabled();   // false when the environment sets CONVGEMM_NO_PDL=1
 
-// Launch, with programmatic stream serialization when `pdl` (and not turned off by
-// CONVGEMM_NO_PDL=1): the kernel must call tc::pdl_wait() before its first global
-// memory access.  Counts the launch.
+// Programmatic dependent launch modes of cg_launch_ex.
+enum CgPdl {
+    CG_PDL_OFF = 0,      // plain launch (the weight-gradient kernels and their reductions)
+    CG_PDL_THREAD = 1,   // as the calling thread's setting says (the persistent chain kernels)
+};
+
+// Launch, with programmatic stream serialization per `pdl` (CgPdl): the kernel must call
+// tc::pdl_wait() before its first global memory access.  Counts the launch.
 template <typename... KArgs, typename... Args>
-cudaError_t cg_launch_ex(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+cudaError_t cg_launch_ex(int pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                          Args &&...args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -67,7 +73,7 @@ cudaError_t cg_launch_ex(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 blo
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = (pdl && cg_pdl_enabled()) ? 1 : 0;
+    cfg.numAttrs = (pdl == CG_PDL_THREAD && cg_pdl_enabled()) ? 1 : 0;
     cg_note_launch();
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...);
 }
@@ -80,7 +86,7 @@ bool cg_wgrad_cluster_enabled();
 template <typename... KArgs, typename... Args>
 cudaError_t cg_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
                           Args &&...args) {
-    return cg_launch_ex(true, kernel, grid, block, smem, st, static_cast<Args &&>(args)...);
+    return cg_launch_ex(CG_PDL_THREAD, kernel, grid, block, smem, st, static_cast<Args &&>(args)...);
 }
 
 

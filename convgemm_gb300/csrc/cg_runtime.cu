@@ -37,13 +37,14 @@ convgemm_status_t cg_cuda_check(cudaError_t e, const char *what) {
 // Programmatic dependent launch for the persistent chain kernels: per host thread,
 // default on unless the environment sets CONVGEMM_NO_PDL=1.
 static thread_local int tl_pdl = -1;
-bool cg_pdl_enabled() {
+bool cg_pdl_env_enabled() {
     static const bool env_on = [] {
         const char *e = getenv("CONVGEMM_NO_PDL");
         return !(e && e[0] == '1');
     }();
-    return tl_pdl < 0 ? env_on : tl_pdl != 0;
+    return env_on;
 }
+bool cg_pdl_enabled() { return tl_pdl < 0 ? cg_pdl_env_enabled() : tl_pdl != 0; }
 extern "C" int convgemm_set_pdl(int on) {
     const int prev = cg_pdl_enabled() ? 1 : 0;
     tl_pdl = on < 0 ? -1 : (on != 0);

@@ -448,7 +448,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     // Weight-gradient work runs beside the forward / input-gradient chain on a side
     // stream: launched without programmatic serialization, so that its grids do not
     // hold SMs early while the persistent chain kernels want them.
-    if (!p.cluster) return cg_launch_ex(false, kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
+    if (!p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
     // the splits of one tile as a cluster along z
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -577,14 +577,14 @@ cudaError_t tc_wgrad_reduce(float *ws, float *dw, int splits, int xa, int Nx, in
         float *gs = ws + (size_t) splits * plane;
         const int per = (splits + groups - 1) / groups;
         dim3 g1((unsigned) ((plane + 255) / 256), groups);
-        if (cudaError_t e = cg_launch_ex(false, wgrad_group_sum_kernel, g1, dim3(256), 0, st, (const float *) ws, gs, splits,
+        if (cudaError_t e = cg_launch_ex(CG_PDL_OFF, wgrad_group_sum_kernel, g1, dim3(256), 0, st, (const float *) ws, gs, splits,
                                          per, plane))
             return e;
         src = gs;
         n = groups;
     }
     dim3 grid((kn + 31) / 32, (Nx + 31) / 32), block(32, 8);
-    return cg_launch_ex(false, wgrad_reduce_kernel, grid, block, 0, st, src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout);
+    return cg_launch_ex(CG_PDL_OFF, wgrad_reduce_kernel, grid, block, 0, st, src, dw, n, xa, Nx, kn, C, Cp, kh * kw, layout);
 }
 
 // ------------------------------------------------------------ bias gradient
