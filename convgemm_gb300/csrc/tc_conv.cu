@@ -85,7 +85,9 @@ struct TcCfg {
     static constexpr int MMA_WARP = EW == 8 ? 1 : 8;
     static constexpr int NCH = BN / CW;   // output chunks of one accumulator
     // TMEM: MT accumulators of BN columns, double-buffered when 512 columns allow
-    static constexpr int ACC_BUFS = 2 * BN * MT <= 512 ? 2 : 1;
+    // (four buffers for tiles of <= 128 columns: their MMAs take ~1.7k cycles, less than the round
+    // trip commit -> epilogue -> TMEM drained -> MMA warp, so two buffers would stall the MMAs)
+    static constexpr int ACC_BUFS = BN * MT <= 128 ? 4 : (2 * BN * MT <= 512 ? 2 : 1);
     static constexpr uint32_t TMEM_COLS = ACC_BUFS * BN * MT;
 };
 
@@ -153,8 +155,8 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     uint64_t *full = (uint64_t *) (epi_smem + C::EPI_BUFS * C::EPI_BYTES);
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
-    uint64_t *acc_empty = acc_full + 2;
-    uint32_t *tmem_holder = (uint32_t *) (acc_empty + 2);
+    uint64_t *acc_empty = acc_full + 4;
+    uint32_t *tmem_holder = (uint32_t *) (acc_empty + 4);
     // per-class tap offsets (packed y:16 | x:16) and the tile's epilogue scale/shift, in shared
     // memory: indexing the kernel parameters with runtime values would go through slow generic loads
     int32_t *tap_tab = (int32_t *) (epi_smem + C::EPI_BUFS * C::EPI_BYTES + 256);
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
             tc::mbar_init(&full[s], IM2C ? 1 : 128 + 1);
             tc::mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < C::ACC_BUFS; b++) {
             tc::mbar_init(&acc_full[b], 1);
             tc::mbar_init(&acc_empty[b], 32 * EW);
         }
@@ -519,26 +521,29 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                     tc::tc_fence_after();
                     const int nkb = min(KB, KT - kt);
                     const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES);
-                    const uint32_t b0 = a0 + C::A_BYTES;
-                    for (int kb = 0; kb < nkb; kb++) {
-                        const uint32_t bb = b0 + kb * C::B_BLOCK;
+                    // descriptors built once per stage; an offset of d bytes adds d / 16 to the
+                    // start field (the stage stays below 256 KB, so the field never carries)
+                    const uint64_t ad0 = op_desc(a0, C::SBO, C::LAYOUT);
+                    const uint64_t bd0 = ad0 + (C::A_BYTES >> 4);
+#pragma unroll
+                    for (int kb = 0; kb < KB; kb++) {
+                        if (kb >= nkb) break;
                         // each MMA consumes 32 bytes of every K row: 16 BF16 or 32 E4M3 elements
 #pragma unroll
                         for (int k = 0; k < C::ROWB / 32; k++) {
                             const uint32_t acc = (kt | kb | k) != 0;
-                            const uint64_t bd = op_desc(bb + k * 32, C::SBO, C::LAYOUT);
+                            const uint64_t bd = bd0 + ((kb * C::B_BLOCK + k * 32) >> 4);
 #pragma unroll
                           for (int mt = 0; mt < MT; mt++) {
-                            const uint32_t ab = a0 + (kb * MT + mt) * C::A_BLOCK;
-                            const uint64_t ad = op_desc(ab + k * 32, C::SBO, C::LAYOUT);
+                            const uint64_t ad = ad0 + (((kb * MT + mt) * C::A_BLOCK + k * 32) >> 4);
                             const uint32_t dtm = dt + (uint32_t) (mt * BN);
                             if (MODE == MODE_FP8) {
                                 tc::mma_f8(dtm, ad, bd, idesc, acc);
                             } else {
                                 tc::mma_f16(dtm, ad, bd, idesc, acc);
                                 if (MODE == MODE_X3) {
-                                    const uint64_t adl = op_desc(ab + C::A_TILE + k * 32, C::SBO, C::LAYOUT);
-                                    const uint64_t bdl = op_desc(bb + C::B_TILE + k * 32, C::SBO, C::LAYOUT);
+                                    const uint64_t adl = ad + (C::A_TILE >> 4);
+                                    const uint64_t bdl = bd + (C::B_TILE >> 4);
                                     tc::mma_f16(dtm, ad, bdl, idesc, 1);   // hi * lo
                                     tc::mma_f16(dtm, adl, bd, idesc, 1);   // lo * hi
                                 }

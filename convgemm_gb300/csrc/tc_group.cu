@@ -222,11 +222,11 @@ __global__ void __launch_bounds__(288, 1)
                         break;
                     }
                     tc::tc_fence_after();
-                    const uint32_t a0 = tc::smem_u32(base + s * STAGE_BYTES), b0 = a0 + A_BYTES;
+                    // descriptors built once per stage; a 32-byte K step adds 2 to the start field
+                    const uint64_t ad = tc::sw128_desc(tc::smem_u32(base + s * STAGE_BYTES), 16, 1024);
+                    const uint64_t bd = ad + (A_BYTES >> 4);
 #pragma unroll
-                    for (int k = 0; k < 4; k++)
-                        tc::mma_f16(dt, tc::sw128_desc(a0 + k * 32, 16, 1024), tc::sw128_desc(b0 + k * 32, 16, 1024),
-                                    idesc, (kt | k) != 0);
+                    for (int k = 0; k < 4; k++) tc::mma_f16(dt, ad + 2 * k, bd + 2 * k, idesc, (kt | k) != 0);
                     tc::mma_commit(&empty[s]);
                 }
                 tc::mma_commit(&acc_full[buf]);

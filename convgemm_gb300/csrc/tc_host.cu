@@ -304,6 +304,11 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
                          const void *in_lo, const void *w_lo, int bn_override, int aux_override,
                          const void *mask, float *stats) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
+    // stride-1 layers with 64-channel blocks and several taps: operands from input slabs, unless the
+    // tuning entry asks for the general kernel (aux bit 8)
+    if (mode == 0 && !mask && !stats && !(aux_override & 8) && tc_slab_applicable(pl) && !((uintptr_t) out & 15) &&
+        !((uintptr_t) in & 15) && !((uintptr_t) wpacked & 15))
+        return tc_slab_run(pl, s, in, wpacked, out, scale, shift, relu, st);
     const int sms = tc_num_sms();
     TcConvParams p;
     memset(&p, 0, sizeof(p));
@@ -373,11 +378,12 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
                 return e;
     }
     // aux (tuning): bits 0-1 the M tiles per weight tile (1 / 2: BF16 im2col path only), bit 2
-    // eight epilogue warps; 0 = heuristic: one M tile, eight epilogue warps when every class
+    // eight epilogue warps, bit 3 (above) the general kernel instead of the slab kernel; bits 0-2
+    // zero = heuristic: one M tile, eight epilogue warps when every class
     // has at most 8 K blocks per tile (the epilogue, not the MMA, bounds such tiles)
     p.mt = ((aux_override & 3) == 2 && mode == 0 && p.im2col) ? 2 : 1;
     bool ew8 = (aux_override & 4) != 0;
-    if (aux_override == 0) {
+    if ((aux_override & 7) == 0) {
         int kmax = 0;
         for (int c = 0; c < pl.ncls; c++) kmax = pl.cls[c].ktiles > kmax ? pl.cls[c].ktiles : kmax;
         ew8 = kmax <= 8;

@@ -31,6 +31,11 @@ bool tc_plan_im2col(TcPlan &pl);
 convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, const unsigned long long *dims,
                                   const unsigned long long *strides_bytes, const unsigned *box, const unsigned *estr,
                                   int swizzle128);
+// Stride-1 convolutions with 64-channel input blocks and 2..16 taps, operands read from
+// input slabs (tc_slab.cu): the forward or input-gradient plan decides.
+bool tc_slab_applicable(const TcPlan &pl);
+convgemm_status_t tc_slab_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
+                              const float *scale, const float *shift, int relu, cudaStream_t st);
 // Forward of convolutions with at most 8 input channels (tc_stem.cu).
 bool tc_stem_applicable(const cg_shape &s);
 convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpacked, int Kpad, void *y,

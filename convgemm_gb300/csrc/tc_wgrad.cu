@@ -276,15 +276,15 @@ __global__ void __launch_bounds__(160, 1)
                 }
                 tc::tc_fence_after();
                 const int nch = min(KB, KT - g * KB);
-                for (int c = 0; c < nch; c++) {
-                    const uint32_t a0 = tc::smem_u32(base + s * C::STAGE_BYTES + c * C::CHUNK_BYTES);
-                    const uint32_t b0 = a0 + C::A_BYTES;
+                // descriptors built once per stage; a 16-row K step (2048 bytes) adds 128 to the start field
+                const uint64_t ad0 = tc::sw128_desc(tc::smem_u32(base + s * C::STAGE_BYTES), 8192, 1024);
 #pragma unroll
-                    for (int k = 0; k < C::BK / 16; k++) {
-                        const uint64_t ad = tc::sw128_desc(a0 + k * 2048, 8192, 1024);
-                        const uint64_t bd = tc::sw128_desc(b0 + k * 2048, 8192, 1024);
-                        tc::mma_f16(tmem, ad, bd, idesc, (g | c | k) != 0);
-                    }
+                for (int c = 0; c < KB; c++) {
+                    if (c >= nch) break;
+                    const uint64_t ad = ad0 + ((c * C::CHUNK_BYTES) >> 4), bd = ad + (C::A_BYTES >> 4);
+#pragma unroll
+                    for (int k = 0; k < C::BK / 16; k++)
+                        tc::mma_f16(tmem, ad + 128 * k, bd + 128 * k, idesc, (g | c | k) != 0);
                 }
                 tc::mma_commit(&empty[s]);
             }

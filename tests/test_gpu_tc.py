@@ -358,3 +358,55 @@ def test_bias_grad_against_fp64(cglib, shape):
     assert torch.equal(db1, db2)
     ref = bf16r(dy).astype(np.float64).reshape(-1, kn).sum(0)
     assert np.abs(db1.cpu().numpy() - ref).max() <= 1e-5 * np.abs(bf16r(dy)).reshape(-1, kn).sum(0).max()
+
+
+SLAB_SHAPES = [
+    # b, h, w, c, kn, k, pad, dil: stride 1, 64-channel blocks -> the slab kernel
+    (2, 14, 14, 64, 64, 3, 1, 1),       # 8 rows of 16 per tile
+    (1, 20, 150, 64, 72, 3, 1, 1),      # two column chunks per row, two N tiles (72 = 64 + 8)
+    (2, 12, 12, 128, 64, 2, 0, 1),      # two channel blocks, 2x2 taps, no padding
+    (1, 16, 40, 64, 64, 3, 2, 2),       # dilation 2
+    (2, 10, 33, 64, 128, 3, 1, 1),      # partial row group at the image bottom (3 + 3 + 3 + 1 rows)
+]
+
+
+@pytest.mark.parametrize("shape", SLAB_SHAPES, ids=[str(s) for s in SLAB_SHAPES])
+def test_slab_kernel_matches_general_kernel_and_fp64(cglib, oracle_lib, shape):
+    """Stride-1 forward and input gradient through the slab kernel are bit-identical to the
+    general kernel (aux + 8 selects it) and within tolerance of FP64."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, dil = shape
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, 1, 1, dil, dil)
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, dil=dil)
+    rng = np.random.default_rng(sum(shape) + 5)
+    K = c * k * k
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    wt = (rng.standard_normal(K * kn) * np.sqrt(2.0 / K)).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    bias = rng.uniform(-.1, .1, kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
+    wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    shift = torch.from_numpy(bias).cuda()
+    outs = []
+    try:
+        for aux in (0, 9):   # default (slab), general kernel
+            tc.tune_set(tc.TUNE_FWD, s, 64 if aux else 0, aux)
+            tc.tune_set(tc.TUNE_DGRAD, s, 64 if aux else 0, aux)
+            y = torch.empty(b, s.ho, s.wo, kn, dtype=torch.bfloat16, device="cuda")
+            dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
+            tc.fwd_bf16(s, xd, wp, y, None, shift, relu=True)
+            tc.dgrad_bf16(s, dyd, wpd, dx)
+            outs.append((y, dx))
+        torch.cuda.synchronize()
+        cg.check_device()
+    finally:
+        tc.tune_clear()
+    assert torch.equal(outs[0][0].view(torch.int16), outs[1][0].view(torch.int16))
+    assert torch.equal(outs[0][1].view(torch.int16), outs[1][1].view(torch.int16))
+    ref = O.fwd_f64(C.NHWC, g, wt, x, {"bias": bias, "relu": True}).ravel()
+    assert rel_max_rms(outs[0][0].float().cpu().numpy().ravel(), ref)[0] <= BF16_TOL
+    ref = O.dgrad_f64(C.NHWC, g, wt, dy).ravel()
+    assert rel_max_rms(outs[0][1].float().cpu().numpy().ravel(), ref)[0] <= BF16_TOL
