@@ -83,10 +83,10 @@ struct TcCfg {
     // warp 8 (EW = 4) or in the otherwise idle warp 1 (EW = 8)
     static constexpr int THREADS = EW == 8 ? 384 : 288;
     static constexpr int MMA_WARP = EW == 8 ? 1 : 8;
+    static constexpr int ISS2_WARP = EW == 8 ? 2 : 1;   // the second MMA issuer (an otherwise idle warp)
     static constexpr int NCH = BN / CW;   // output chunks of one accumulator
-    // TMEM: MT accumulators of BN columns, double-buffered when 512 columns allow
-    // (four buffers for tiles of <= 128 columns: their MMAs take ~1.7k cycles, less than the round
-    // trip commit -> epilogue -> TMEM drained -> MMA warp, so two buffers would stall the MMAs)
+    // TMEM: MT accumulators of BN columns, double-buffered when 512 columns allow (four buffers
+    // for tiles of <= 128 columns)
     static constexpr int ACC_BUFS = BN * MT <= 128 ? 4 : (2 * BN * MT <= 512 ? 2 : 1);
     static constexpr uint32_t TMEM_COLS = ACC_BUFS * BN * MT;
 };
@@ -147,6 +147,10 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                    const __grid_constant__ CUtensorMap omap, const __grid_constant__ TcMaps amaps) {
     using C = TcCfg<BN, STAGES, KB, MODE, MT, EW>;
     static_assert(EW == 4 || (IM2C && MT * C::NCH >= 2), "eight epilogue warps: im2col path, two chunks or more");
+    // Two MMA-issuing threads on the BF16 im2col path: one per M tile (MT = 2), or one per N half
+    // (MT = 1, BN >= 128).  One thread's instruction stream issues N <= 128 MMAs more slowly than the
+    // tensor core runs them; both wait for the same stage and commit to it.
+    constexpr bool SPLIT = IM2C && MODE == MODE_BF16 && (MT == 2 || BN >= 128);
     static_assert(IM2C || (KB == 1 && MODE == MODE_BF16), "the cp.async gather fills one BF16 K block per stage");
     static_assert(MT == 1 || (IM2C && MODE == MODE_BF16), "two M tiles per weight tile: BF16 im2col path only");
     extern __shared__ uint8_t smem_raw[];
@@ -170,10 +174,10 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
         for (int s = 0; s < STAGES; s++) {
             // im2col: the one expect_tx arrival; gather: 128 producer threads + the expect_tx
             tc::mbar_init(&full[s], IM2C ? 1 : 128 + 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], SPLIT ? 2 : 1);
         }
         for (int b = 0; b < C::ACC_BUFS; b++) {
-            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_full[b], SPLIT ? 2 : 1);
             tc::mbar_init(&acc_empty[b], 32 * EW);
         }
         tc::fence_mbar_init();
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     const uint32_t tmem = *tmem_holder;
     bool ok = true;
 
-    if (IM2C && warp < 4 && warp != C::MMA_WARP) {
+    if (IM2C && warp < 4 && warp != C::MMA_WARP && !(SPLIT && warp == C::ISS2_WARP)) {
         // ------------------------------------------------ producer: one thread, im2col TMA for A, TMA for B
         if (threadIdx.x == 0) {
             uint32_t it = 0;
@@ -499,7 +503,12 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
     } else {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = MODE == MODE_FP8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, BN, 0, 0);
+            // issuer `me`: its M tile (MT = 2) or N half (MT = 1) when SPLIT, else everything
+            const int me = (SPLIT && warp == C::ISS2_WARP) ? 1 : 0;
+            constexpr int NI = (SPLIT && MT == 1) ? BN / 2 : BN;   // N of one MMA instruction
+            constexpr uint32_t idesc = MODE == MODE_FP8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, NI, 0, 0);
+            const uint32_t n_off = (SPLIT && MT == 1) ? (uint32_t) (me * NI) : 0u;   // accumulator column
+            const uint64_t b_off = (SPLIT && MT == 1) ? (uint64_t) (me * NI * C::ROWB) >> 4 : 0u;   // B rows
             uint32_t it = 0, lt = 0;
             for (int tile = blockIdx.x; tile < p.ntiles_total && ok; tile += gridDim.x, lt++) {
                 const Tile tl = decode_tile(cls_tab, p.ncls, p.ntiles, BN, tile, MT);
@@ -532,11 +541,12 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
 #pragma unroll
                         for (int k = 0; k < C::ROWB / 32; k++) {
                             const uint32_t acc = (kt | kb | k) != 0;
-                            const uint64_t bd = bd0 + ((kb * C::B_BLOCK + k * 32) >> 4);
+                            const uint64_t bd = bd0 + ((kb * C::B_BLOCK + k * 32) >> 4) + b_off;
 #pragma unroll
                           for (int mt = 0; mt < MT; mt++) {
+                            if (SPLIT && MT == 2 && mt != me) continue;
                             const uint64_t ad = ad0 + (((kb * MT + mt) * C::A_BLOCK + k * 32) >> 4);
-                            const uint32_t dtm = dt + (uint32_t) (mt * BN);
+                            const uint32_t dtm = dt + (uint32_t) (mt * BN) + n_off;
                             if (MODE == MODE_FP8) {
                                 tc::mma_f8(dtm, ad, bd, idesc, acc);
                             } else {
