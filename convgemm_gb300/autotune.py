@@ -197,7 +197,19 @@ def op_candidates(op: int, s):
     widths = [64, 128] if s.kn < 128 else candidate_widths(s.kh * s.kw * tc.c8(s.c))
     # around the heuristic, plus the cluster-reduced split counts (2..8) that fit
     splits = sorted({max(1, s0 // 4), max(1, s0 // 2), s0, min(mx, 2 * s0)} | {x for x in (2, 4, 8) if x <= mx})
-    return [(w, sp) for w in widths for sp in splits]
+    out = [(w, sp) for w in widths for sp in splits]
+    if tc.c8(s.c) % 64 == 0:
+        one = s.kh == 1 and s.kw == 1 and s.vstride == 1 and s.hstride == 1 and s.vpad == 0 and s.hpad == 0
+        if one:   # the same tiling with X by im2col boxes instead of tiled boxes
+            out += [(w, s0 | tc.WGRAD_IM2COL_X) for w in widths]
+        if s.kn >= 128:   # X as the A operand of a wide layer, around its own split heuristic
+            for w in (128, 256) if s.kn >= 256 else (128,):
+                tc.tune_set(op, s, w, tc.WGRAD_X_ON_A)
+                _, s2, _ = tc.wgrad_bf16_plan(s)
+                for sp in sorted({max(1, s2 // 2), s2, min(mx, 2 * s2)} | {x for x in (2, 4, 8) if x <= mx}):
+                    out.append((w, sp | tc.WGRAD_X_ON_A))
+            tc.tune_set(op, s, 0, 0)
+    return out
 
 
 def tune_ops(items, path: str | None = None, force: bool = False, measure_missing: bool = True,

@@ -543,9 +543,17 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *sh
 namespace {
 
 struct WgPlan {
-    int xa, bn, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
+    int xa, bn, x2d, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
     size_t ws_bytes;
 };
+
+// Whether the weight gradient gathers X with im2col TMA (channels in 64-element atoms,
+// padding and far-edge offsets within the im2col map's signed 8-bit corners).
+bool wgrad_im2col_ok(const cg_shape &s, const ConvGeom &g) {
+    const int up_h = -s.vpad + (g.ho - 1) * s.vstride - (s.h - 1), up_w = -s.hpad + (g.wo - 1) * s.hstride - (s.w - 1);
+    return (round_up(s.c, 8) % 64) == 0 && s.vpad <= 128 && s.hpad <= 128 && up_h >= -128 && up_h <= 127 &&
+           up_w >= -128 && up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
+}
 
 WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     const cg_shape s = cg_from_public(ps);
@@ -556,13 +564,20 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.Cp = round_up(s.c, 8);
     w.kn8 = round_up(s.kn, 8);
     w.Nx = s.kh * s.kw * w.Cp;
-    w.xa = s.kn < 128;
+    const bool im2col = wgrad_im2col_ok(s, g);
+    const int aux_splits = t.splits & 0xffff;
+    // X on the A side: always for narrow layers, on request for wide ones (im2col path)
+    const bool x_on_a = (t.splits & CONVGEMM_WGRAD_X_ON_A) && im2col;
+    w.xa = s.kn < 128 || x_on_a;
+    // X of a 1x1 stride-1 unpadded convolution is a plain [P][Cp] matrix: tiled boxes
+    w.x2d = im2col && s.kh == 1 && s.kw == 1 && s.vstride == 1 && s.hstride == 1 && s.vpad == 0 && s.hpad == 0 &&
+            !(t.splits & CONVGEMM_WGRAD_IM2COL_X);
     int Mext, Next;
     if (w.xa) {
         Mext = w.Nx;
         Next = s.kn;
-        w.bn = s.kn <= 64 ? 64 : 128;
-        if (t.bn == 64 || t.bn == 128) w.bn = t.bn;
+        w.bn = s.kn <= 64 ? 64 : (s.kn >= 256 && x_on_a ? 256 : 128);
+        if (t.bn == 64 || t.bn == 128 || (t.bn == 256 && x_on_a)) w.bn = t.bn;
     } else {
         Mext = s.kn;
         Next = w.Nx;
@@ -577,7 +592,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     int splits = tc_num_sms() * per_sm / base;   // one wave: no partial second wave
     const int max_splits = (w.nchunks + 7) / 8;  // at least 8 chunks (512 pixels) per split
     if (splits > max_splits) splits = max_splits;
-    if (t.splits) splits = t.splits < w.nchunks ? t.splits : w.nchunks;
+    if (aux_splits) splits = aux_splits < w.nchunks ? aux_splits : w.nchunks;
     if (splits < 1) splits = 1;
     w.cps = (w.nchunks + splits - 1) / splits;
     w.splits = (w.nchunks + w.cps - 1) / w.cps;
@@ -649,12 +664,16 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     memset(&xmap, 0, sizeof(xmap));
     {
         const int up_h = -s.vpad + (g.ho - 1) * s.vstride - (s.h - 1), up_w = -s.hpad + (g.wo - 1) * s.hstride - (s.w - 1);
-        p.im2col = (p.Cp % 64) == 0 && s.vpad <= 128 && s.hpad <= 128 && up_h >= -128 && up_h <= 127 && up_w >= -128 &&
-                   up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
-        if (p.im2col)
+        p.im2col = wgrad_im2col_ok(s, g);
+        p.x2d = w.x2d;
+        if (p.x2d) {
+            if (convgemm_status_t e = tc_make_map_2d(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, x, g.P, p.Cp, 64, 64))
+                return e;
+        } else if (p.im2col) {
             if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
                                                          s.vstride, s.hstride, 64, 2))
                 return e;
+        }
     }
     cudaStream_t st = (cudaStream_t) stream;
     // one split: the kernel writes dW itself

@@ -36,13 +36,14 @@ extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *s
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_tune_set: tile width %d is not 0/64/128/256", bn);
     const bool mt_op = op == CONVGEMM_TUNE_FWD || op == CONVGEMM_TUNE_DGRAD;
     // forward / input gradient: M tiles per weight tile (1 / 2) + 4 for eight epilogue warps
-    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? splits >= 0
+    // weight gradient: pixel splits in bits 0-15, CONVGEMM_WGRAD_* flags above
+    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? (splits >= 0 && (splits & ~0x3ffff) == 0)
                         : mt_op ? ((splits & ~8) == 0 || (splits & ~8) == 1 || (splits & ~8) == 2 ||
                                    (splits & ~8) == 5 || (splits & ~8) == 6)
                                 : splits == 0;
     if (!aux_ok)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE,
-                            "convgemm_tune_set: aux is the weight gradient's split count, or for the BF16 forward / "
+                            "convgemm_tune_set: aux is the weight gradient's split count (plus CONVGEMM_WGRAD_* flags), or for the BF16 forward / "
                             "input gradient 1 / 2 M tiles per weight tile, plus 4 for eight epilogue warps, plus 8 for the general "
                             "kernel instead of the slab kernel");
     std::lock_guard<std::mutex> lk(g_tune_mu);

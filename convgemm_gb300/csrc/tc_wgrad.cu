@@ -11,10 +11,15 @@
 // Both operands reach the tensor core MN-major (the pixel index is the slow,
 // K dimension in memory):
 //   dY side: TMA boxes of 64 channels x 64 pixels from dY viewed as [P][kn8];
-//   X side:  16-byte cp.async gathers of 8 channels of one tap for each pixel,
-//            zero-filled for padding, written in the 128-byte-swizzled layout.
+//   X side:  im2col-mode TMA boxes of 64 channels of one tap x 64 pixels when the
+//            channels are multiples of 64 (tiled boxes of the [P][Cp] matrix for a
+//            1x1 stride-1 unpadded convolution), else 16-byte cp.async gathers of
+//            8 channels of one tap for each pixel, zero-filled for padding, written
+//            in the 128-byte-swizzled layout.
 // The X side is the 128-row A operand when kn < 128 (template XA), else dY is,
-// so narrow layers do not waste half of each MMA.
+// so narrow layers do not waste half of each MMA; a tuned configuration may put
+// the X side on A for wide layers too (measured faster on 3x3 layers at the same
+// tile shape and traffic).
 #include <cuda_bf16.h>
 
 #include "cg_common.cuh"
@@ -117,9 +122,13 @@ __global__ void __launch_bounds__(160, 1)
                     const int h0 = (int) oh * p.vstr - p.vpad, w0 = (int) ow * p.hstr - p.hpad;
                     const uint32_t st0 = tc::smem_u32(base + s * C::STAGE_BYTES + c * C::CHUNK_BYTES);
 #pragma unroll
-                    for (int a = 0; a < C::X_ATOMS; a++)
-                        tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
-                                               a_oy[a], &full[s]);
+                    for (int a = 0; a < C::X_ATOMS; a++) {
+                        if (p.x2d)   // one tap: the atom's channels are columns a_ci of the [P][Cp] matrix
+                            tc::tma_load_2d(st0 + xoff + a * 8192, &xmap, a_ci[a], pbase, &full[s]);
+                        else
+                            tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
+                                                   a_oy[a], &full[s]);
+                    }
 #pragma unroll
                     for (int a = 0; a < C::DY_ATOMS; a++)
                         tc::tma_load_2d(st0 + dyoff + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
@@ -172,7 +181,8 @@ __global__ void __launch_bounds__(160, 1)
                     const int iy = iy0 + a_oy[a], ix = ix0 + a_ox[a];
                     const bool v = bb >= 0 && a_ok[a] && (unsigned) iy < (unsigned) p.H && (unsigned) ix < (unsigned) p.W;
                     const bf16 *src = v ? p.x + ((((size_t) bb * p.H + iy) * p.W + ix) * p.Cp + a_ci[a]) : p.x;
-                    tc::cp_async_16(sX + a * 8192 + r * 128 + ((piece ^ (r & 7)) << 4), src, v ? 16u : 0u);
+                    // L1-cached: a piece is re-read by the neighbouring taps and pixels
+                    tc::cp_async_16_ca(sX + a * 8192 + r * 128 + ((piece ^ (r & 7)) << 4), src, v ? 16u : 0u);
                 }
             }
             tc::cp_async_commit();
@@ -509,6 +519,7 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
             switch (bn) {
                 case 64: return launch_wg<64, 2, true, IM2C, 2>(p, dymap, xmap, grid, st);
                 case 128: return launch_wg<128, 3, true, IM2C, 2>(p, dymap, xmap, grid, st);
+                case 256: return launch_wg<256, 2, true, IM2C, 2>(p, dymap, xmap, grid, st);
                 default: return cudaErrorInvalidValue;
             }
         }
@@ -540,8 +551,9 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
 bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits) {
     if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;
     if (im2col) {
-        if (xa) return bn == 64 ? cluster_fits<64, 2, true, true, 2>(splits)
-                                : bn == 128 && cluster_fits<128, 3, true, true, 2>(splits);
+        if (xa) return bn == 64    ? cluster_fits<64, 2, true, true, 2>(splits)
+                       : bn == 128 ? cluster_fits<128, 3, true, true, 2>(splits)
+                                   : bn == 256 && cluster_fits<256, 2, true, true, 2>(splits);
         return bn == 64    ? cluster_fits<64, 2, false, true, 2>(splits)
                : bn == 128 ? cluster_fits<128, 3, false, true, 2>(splits)
                            : bn == 256 && cluster_fits<256, 2, false, true, 2>(splits);

@@ -14,6 +14,8 @@ struct TcWgradParams {
     FastDiv dcp, dwo, dho;
     int *err;
     int im2col;               // X by im2col-mode TMA (Cp % 64 == 0), else by cp.async gathers
+    int x2d;                  // with im2col: X of a 1x1 stride-1 unpadded convolution is the matrix
+                              // [P][Cp], loaded by tiled TMA (xmap 2-D, 64 x 64 boxes) instead
     // one split: the epilogue writes dW itself (no workspace, no reduction) in the
     // reference layout `layout` (0: [ci][kh][kw][co], 1: [co][ci][kh][kw]) of C channels
     float *dw;

@@ -103,6 +103,8 @@ def wgrad_bf16_plan(shape: Shape):
 
 
 TUNE_FWD, TUNE_DGRAD, TUNE_WGRAD, TUNE_FWD_FP8, TUNE_FWD_BF16X3 = range(5)
+WGRAD_X_ON_A = 0x10000      # weight-gradient aux flags: X as the A operand of a wide layer,
+WGRAD_IM2COL_X = 0x20000    # X of a 1x1 stride-1 unpadded layer by im2col instead of tiled boxes
 
 
 def tune_set(op: int, shape: Shape, bn: int = 0, splits: int = 0):

@@ -221,12 +221,20 @@ enum {
 /* Process-wide override of the built-in heuristics for one operation on one
  * shape, as chosen by an autotuner: bn = output channels per tile (64, 128 or
  * 256; for the weight gradient the width of its N side); aux = pixel splits of
- * the weight gradient, or, for the BF16 forward / input gradient, the number of
+ * the weight gradient (bits 0-15; 0 = heuristic) plus the CONVGEMM_WGRAD_* flags
+ * below, or, for the BF16 forward / input gradient, the number of
  * 128-row M tiles (1 or 2) that share each weight tile, plus 4 for the kernel
  * form with eight epilogue warps (short-K layers; 0 = heuristic).
  * bn = aux = 0 removes the entry.  Set the weight-gradient entry before querying
  * its workspace size.  Thread-safe. */
 convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int aux);
+/* Weight-gradient flags (channels that are multiples of 64): X, not dY, as the
+ * 128-row A operand of a layer with kn >= 128 (N widths 64 / 128 / 256 of kn);
+ * X of a 1x1 stride-1 unpadded convolution by im2col boxes instead of tiled
+ * boxes of the [pixels][channels] matrix.  Results equal the default's within
+ * the BF16 bound (the tiled / im2col choice gives the same bits). */
+#define CONVGEMM_WGRAD_X_ON_A 0x10000
+#define CONVGEMM_WGRAD_IM2COL_X 0x20000
 void convgemm_tune_clear(void);
 
 /* ----------------------------------------- grouped persistent forward launch */

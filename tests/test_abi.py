@@ -108,6 +108,8 @@ def test_tune_table_validation_without_gpu(cglib):
     assert L.convgemm_tune_set(tc.TUNE_DGRAD, ctypes.byref(s), 128, 6) == 0    # 2 M tiles, 8 epilogue warps
     assert L.convgemm_tune_set(tc.TUNE_FWD_FP8, ctypes.byref(s), 128, 1) == 1
     assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 0, 3) == 0
+    assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 256, 3 | tc.WGRAD_X_ON_A | tc.WGRAD_IM2COL_X) == 0
+    assert L.convgemm_tune_set(tc.TUNE_WGRAD, ctypes.byref(s), 256, 0x40000) == 1   # no such flag
     tc.tune_clear()
 
 

@@ -239,6 +239,52 @@ def test_tuned_tile_configurations_agree(cglib, oracle_lib):
         tc.tune_clear()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("b,h,w,c,kn,k,st,pad", [(4, 14, 14, 128, 192, 3, 1, 1), (4, 14, 14, 128, 256, 1, 1, 0),
+                                                 (8, 9, 9, 256, 320, 1, 2, 0), (4, 15, 13, 64, 64, 1, 1, 0)])
+def test_wgrad_operand_forms(cglib, oracle_lib, b, h, w, c, kn, k, st, pad):
+    """The weight gradient's operand forms: X of a 1x1 stride-1 layer by tiled boxes (the
+    default) or by im2col boxes gives the same bits; X as the A operand of a wide layer, with
+    N tiles of 128 / 256 channels (partial last tile included), stays within the BF16 bound."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, st, st)
+    g = C.geom(b, h, w, c, kn, k, k, stride=st, pad=pad)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(79)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * ho * wo * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, ho, wo)
+    ref = O.wgrad_f64(C.NHWC, g, dy, x)
+    one = k == 1 and st == 1 and pad == 0
+
+    def run(bn, aux):
+        tc.tune_set(tc.TUNE_WGRAD, s, bn, aux)
+        plan = tc.wgrad_bf16_plan(s)[:2]
+        ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+        d = torch.empty(k * k * c * kn, device="cuda")
+        tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d, ws)
+        torch.cuda.synchronize()
+        cg.check_device()
+        return plan, d.cpu().numpy()
+
+    try:
+        for splits in (1, 3, 64):   # 64: one 64-pixel chunk per split (capped by the chunk count)
+            p0, d0 = run(0, splits)
+            assert rel_max_rms(d0, ref)[0] <= BF16_TOL
+            if one:
+                p1, d1 = run(0, splits | tc.WGRAD_IM2COL_X)
+                assert p1 == p0 and np.array_equal(d0, d1), (splits, p0)
+            if kn >= 128:
+                for bn in (128, 256):
+                    p2, d2 = run(bn, splits | tc.WGRAD_X_ON_A)
+                    assert p2[0] == bn
+                    assert rel_max_rms(d2, ref)[0] <= BF16_TOL, (bn, p2)
+    finally:
+        tc.tune_clear()
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc
