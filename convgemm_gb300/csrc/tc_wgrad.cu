@@ -47,8 +47,16 @@ struct WgCfg {
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
 };
 
+// Warps: the gather warps (one TMA-issuing thread on the im2col path; eight warps of
+// cp.async gathers otherwise, whose issue rate bounds that path), then the MMA warp;
+// warps 0-3 run the epilogue.
+template <bool IM2C>
+struct WgWarps {
+    static constexpr int GW = IM2C ? 4 : 8, THREADS = 32 * (GW + 1);
+};
+
 template <int BN, int STAGES, bool XA, bool IM2C, int KB>
-__global__ void __launch_bounds__(160, 1)
+__global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
     tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
                     const __grid_constant__ CUtensorMap xmap) {
     using C = WgCfg<BN, STAGES, XA, KB>;
@@ -60,10 +68,11 @@ __global__ void __launch_bounds__(160, 1)
     uint64_t *accum = empty + STAGES;
     uint32_t *tmem_holder = (uint32_t *) (accum + 1);
 
+    constexpr int GW = WgWarps<IM2C>::GW;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            tc::mbar_init(&full[s], IM2C ? 1 : 128 + 1);
+            tc::mbar_init(&full[s], IM2C ? 1 : 32 * GW + 1);
             tc::mbar_init(&empty[s], 1);
         }
         tc::mbar_init(accum, 1);
@@ -71,7 +80,7 @@ __global__ void __launch_bounds__(160, 1)
         tc::prefetch_tmap(&dymap);
         if (IM2C) tc::prefetch_tmap(&xmap);
     }
-    if (warp == 4) {
+    if (warp == GW) {
         tc::tmem_alloc(tmem_holder, BN);
         tc::tmem_relinquish();
     }
@@ -136,10 +145,11 @@ __global__ void __launch_bounds__(160, 1)
             }
         }
         // epilogue below runs on all four warps
-    } else if (warp < 4) {
+    } else if (warp < GW) {
         const int t = threadIdx.x;
         const int piece = t & 7;
-        const int r0 = t >> 3;  // pixel rows r0 + 16*i, i < 4
+        constexpr int RSTEP = 4 * GW;   // pixel rows r0 + RSTEP*i, i < 64 / RSTEP
+        const int r0 = t >> 3;
         // per X atom: the tap and channel of this thread's 8-channel piece (fixed for the CTA)
         int a_ci[C::X_ATOMS], a_oy[C::X_ATOMS], a_ox[C::X_ATOMS];
         bool a_ok[C::X_ATOMS];
@@ -164,8 +174,8 @@ __global__ void __launch_bounds__(160, 1)
             const int pbase = (chunk0 + kt) * C::BK;
             const uint32_t sX = tc::smem_u32(base + s * C::STAGE_BYTES + xoff);
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const int r = r0 + 16 * i;
+            for (int i = 0; i < 64 / RSTEP; i++) {
+                const int r = r0 + RSTEP * i;
                 const int pix = pbase + r;
                 int bb = -1, iy0 = 0, ix0 = 0;
                 if (pix < p.P) {
@@ -274,7 +284,7 @@ __global__ void __launch_bounds__(160, 1)
                 }
             }
         }
-    } else {
+    } else if (warp == GW) {
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
             for (int g = 0; g < NG; g++) {
@@ -357,7 +367,7 @@ __global__ void __launch_bounds__(160, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 4) tc::tmem_dealloc(tmem, BN);
+    if (warp == GW) tc::tmem_dealloc(tmem, BN);
 }
 
 // First pass of the reduction when there are many splits: group g sums the
@@ -458,11 +468,12 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     // Weight-gradient work runs beside the forward / input-gradient chain on a side
     // stream: launched without programmatic serialization, so that its grids do not
     // hold SMs early while the persistent chain kernels want them.
-    if (!p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(160), C::SMEM, st, p, map, xmap);
+    constexpr int THREADS = WgWarps<IM2C>::THREADS;
+    if (!p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(THREADS), C::SMEM, st, p, map, xmap);
     // the splits of one tile as a cluster along z
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
-    cfg.blockDim = dim3(160);
+    cfg.blockDim = dim3(THREADS);
     cfg.dynamicSmemBytes = C::SMEM;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
@@ -490,7 +501,7 @@ bool cluster_fits(int splits) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(1, 1, splits);
-        cfg.blockDim = dim3(160);
+        cfg.blockDim = dim3(WgWarps<IM2C>::THREADS);
         cfg.dynamicSmemBytes = C::SMEM;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
