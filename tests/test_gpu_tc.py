@@ -138,6 +138,9 @@ WGRAD_SHAPES = [
     (2, 9, 9, 16, 256, 1, 0, 2, 1),       # Nx = 16: BN = 64 on the X side
     (8, 56, 56, 64, 256, 1, 0, 1, 1),     # 49 splits: two-pass grouped reduction, dY is A
     (8, 56, 56, 256, 64, 1, 0, 1, 1),     # 49 splits, X is A
+    (2, 17, 19, 8, 96, 3, 1, 1, 1),       # 8 channels: one 8-channel im2col box per tap, BN = 128
+    (2, 16, 16, 5, 64, 5, 2, 1, 2),       # 5 channels padded to 8, dilation 2
+    (1, 9, 9, 8, 64, 1, 0, 1, 1),         # 8 channels, 1x1: Nx = 8, one tap
 ]
 
 
