@@ -543,7 +543,7 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *sh
 namespace {
 
 struct WgPlan {
-    int xa, bn, x2d, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
+    int xa, bn, x2d, stem, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
     size_t ws_bytes;
 };
 
@@ -596,6 +596,11 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     if (splits < 1) splits = 1;
     w.cps = (w.nchunks + splits - 1) / splits;
     w.splits = (w.nchunks + w.cps - 1) / w.cps;
+    w.stem = tc_stem_wgrad_applicable(s);
+    if (w.stem) {   // the slab kernel: one partial per CTA, tile settings do not apply
+        w.bn = 64;
+        w.splits = tc_stem_wgrad_splits(s);
+    }
     w.ws_bytes = sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
     return w;
 }
@@ -631,6 +636,8 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     if (workspace_bytes < w.ws_bytes)
         return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "convgemm_wgrad_bf16: workspace %zu bytes < %zu needed",
                             workspace_bytes, w.ws_bytes);
+    if (w.stem)
+        return tc_stem_wgrad_run(s, dy, x, (float *) workspace, dw, layout == CONVGEMM_NCHW, (cudaStream_t) stream);
     CUtensorMap map;
     if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, w.kn8, 64, 64))
         return e;

@@ -45,6 +45,14 @@ convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpac
 int tc_stem_stat_groups(const cg_shape &s);
 
 int tc_num_sms();
+// Weight gradient of stride-2 convolutions with c <= 8 and kn == 64 (the ResNet stem) from
+// input slabs: applicability, the number of FP32 partials (workspace planes before the
+// reduction's groups), and the run (partials into ws, then the fixed-order reduction into dw
+// in layout 0 NHWC-API / 1 NCHW-API).
+bool tc_stem_wgrad_applicable(const cg_shape &s);
+int tc_stem_wgrad_splits(const cg_shape &s);
+convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const void *x, float *ws, float *dw,
+                                    int layout, cudaStream_t st);
 // Autotuned tile configuration of one operation on one shape (0 = heuristic):
 // bn = output channels per tile; splits = pixel splits of the weight gradient,
 // or M tiles per weight tile (1 or 2) of the forward / input gradient.

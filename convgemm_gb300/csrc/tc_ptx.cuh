@@ -113,6 +113,22 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         "l"((uint64_t) map), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(dst),
+        "l"((uint64_t) map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"((uint64_t) map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
 // im2col-mode load of a 4-D NHWC tensor: pixelsPerColumn pixels starting at
 // (w, h, n) inside the map's bounding box, channelsPerPixel channels from c,
 // each pixel displaced by the filter offset (ow, oh); outside the tensor -> 0.
@@ -197,6 +213,18 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr, uint32_t lbo_byte
     d |= (uint64_t) ((sbo_bytes >> 4) & 0x3FFF) << 32;
     d |= (uint64_t) 1 << 46;   // descriptor version for tcgen05
     d |= (uint64_t) 2 << 61;   // SWIZZLE_128B
+    return d;
+}
+
+// Shared-memory matrix descriptor, no swizzle, MN-major operand: core matrices of
+// 8 M/N elements (16 B) x 8 K rows (16 B apart, 128 B each); 8-row K groups LBO
+// apart, 8-element M/N groups SBO apart.
+__device__ __forceinline__ uint64_t mn_interleave_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
+    uint64_t d = 0;
+    d |= (uint64_t) ((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t) ((lbo_bytes >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t) ((sbo_bytes >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t) 1 << 46;   // descriptor version for tcgen05; layout bits 61-63 = 0: no swizzle
     return d;
 }
 

@@ -141,6 +141,9 @@ WGRAD_SHAPES = [
     (2, 17, 19, 8, 96, 3, 1, 1, 1),       # 8 channels: one 8-channel im2col box per tap, BN = 128
     (2, 16, 16, 5, 64, 5, 2, 1, 2),       # 5 channels padded to 8, dilation 2
     (1, 9, 9, 8, 64, 1, 0, 1, 1),         # 8 channels, 1x1: Nx = 8, one tap
+    (1, 224, 224, 3, 64, 7, 3, 2, 1),     # the ResNet-50 stem: slab kernel, 28 bands of 4 output rows
+    (2, 30, 26, 8, 64, 5, 2, 2, 1),       # slab kernel: even padding, 3 tap pairs, last band of 3 rows
+    (1, 19, 17, 6, 64, 3, 1, 2, 1),       # slab kernel: 3x3, 2 tap pairs
 ]
 
 
@@ -175,6 +178,20 @@ def test_wgrad_bf16_against_fp64(cglib, oracle_lib, shape):
     assert rel_max_rms(got_nchw, O.wgrad_f64(C.NCHW, g, np.ascontiguousarray(
         bf16r(dy).reshape(b, s.ho, s.wo, kn).transpose(0, 3, 1, 2)).ravel(), np.ascontiguousarray(
         bf16r(x).reshape(b, h, w, c).transpose(0, 3, 1, 2)).ravel()))[0] <= 1e-4
+
+
+def test_wgrad_stem_uses_slab_kernel(cglib):
+    """The ResNet-50 stem's weight gradient plans one FP32 partial per CTA of the slab kernel
+    (bands of 4 output rows), whatever tile configuration is set for it."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    s = cg.Shape.of(64, 224, 224, 3, 64, 7, 7, 3, 3, 2, 2)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    try:
+        tc.tune_set(tc.TUNE_WGRAD, s, 128, 7)
+        assert tc.wgrad_bf16_plan(s)[:2] == (64, min(sms, 64 * 28))
+    finally:
+        tc.tune_clear()
 
 
 def test_wgrad_bf16_rejects_small_workspace(cglib):
