@@ -8,8 +8,8 @@
 // (16-byte cp.async per pixel and tap) bounds the general kernel.  Here the tensor core
 // reads its A operand (M = n, K = pixels, MN-major) straight out of input slabs:
 //   * a CTA takes bands of SW_R output rows of one image; for every input row of the band
-//     (2*SW_R + 6 of them: kernel rows up to 8) and each of two column streams, one TMA
-//     load with traversal stride 2 brings the slab row
+//     (2*(SW_R-1) + kh of them) and each of two column streams, one TMA load with traversal
+//     stride 2 brings the slab row
 //         S[2*y + st][s] = x[b][2*oy0 - pad_h + y][col0[st] + 2*s][0..7],  s < ent,
 //     col0[0] = 1 - pad_w (taps kx = 2m+1), col0[1] = -pad_w (taps kx = 2m), so that tap
 //     pair m at output column ox reads entry s = ox + m of both streams;
@@ -17,10 +17,13 @@
 //     8 channels x 8 pixels each, no swizzle) of pair m start at slab row 4*r and are one
 //     slab row apart (SBO = the row pitch), 8-pixel K groups 128 bytes apart (LBO): one
 //     M=128 MMA per pair and 16-pixel K step, four TMEM accumulators of 64 columns;
-//   * dY of the band arrives as one tiled box (64 channels x Wpad pixels x SW_R rows,
-//     128-byte swizzle), the B operand, pixels past Wo zero-filled;
-//   * stages (slab rows + dY) are double-buffered across bands; kernel rows 7 (for kh = 7)
-//     and taps kx >= kw are computed and dropped;
+//   * a 16-byte TMA box row is one TMA element and the engine's element rate bounds these
+//     loads, so bands are tall (each input row is loaded by 2 of the band's 8 output rows'
+//     worth of work instead of 3.5) and slab stages are double-buffered across bands;
+//   * dY arrives per output row (64 channels x Wpad pixels, 128-byte swizzle, pixels past
+//     Wo zero-filled) through a ring of SW_DYB buffers filled by a second producer warp;
+//   * kernel rows >= kh (their slab rows are not loaded: stale data) and taps kx >= kw
+//     are computed and dropped;
 //   * each CTA writes its FP32 partial [n][co] to the workspace; the fixed-order split
 //     reduction of the general kernel adds the partials in CTA order and writes dW.
 #include <cstring>
@@ -34,42 +37,50 @@
 
 namespace {
 
-constexpr int SW_R = 4;                          // output rows per band
-constexpr int SW_NY = 2 * SW_R + 6;              // input rows per band (kernel rows 0..7)
+constexpr int SW_R = 8;                          // output rows per band
+constexpr int SW_NY = 2 * SW_R + 6;              // slab rows per stream and stage (kernel rows 0..7)
 constexpr int SW_MAXPAIRS = 4;                   // kw <= 8
-constexpr uint32_t SW_SLAB_MAX = 56 * 1024;      // 2 * SW_NY slab rows of one stage
-constexpr uint32_t SW_DY_MAX = 56 * 1024;        // SW_R rows x Wpad pixels x 128 B of dY
-constexpr uint32_t SW_STAGE = SW_SLAB_MAX + SW_DY_MAX;
-constexpr size_t SW_SMEM = 1024 + 2 * (size_t) SW_STAGE + 256;
+constexpr uint32_t SW_SLAB_MAX = 83 * 1024;      // 2 * SW_NY slab rows of one stage
+constexpr int SW_DYB = 3;                        // dY row buffers
+constexpr uint32_t SW_DY_MAX = 16 * 1024;        // one output row of dY: Wpad pixels x 128 B
+constexpr size_t SW_SMEM = 1024 + 2 * (size_t) SW_SLAB_MAX + SW_DYB * (size_t) SW_DY_MAX + 256;
 static_assert(SW_SMEM <= 232448, "shared memory");
 
 struct StemWgParams {
     float *ws;                 // [gridDim.x][Nx][64] FP32 partials, Nx = kh * kw * 8
-    int Ho, kh, kw, pad_h, npairs, nks, wpad;
+    int Ho, kh, kw, pad_h, npairs, nks, wpad, nyl;   // nyl: input rows loaded per band
     int bands_per_img, total_bands;
     int col0[2];               // input column of slab entry 0 of stream 0 / 1
     uint32_t pitch;            // bytes per slab row (entries * 16, rounded up to 128)
-    uint32_t tx;               // bytes the TMA loads of one stage deliver
+    uint32_t tx;               // bytes the slab loads of one stage deliver
     int *err;
 };
 
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(256, 1)
     tc_stem_wgrad_kernel(const __grid_constant__ StemWgParams p, const __grid_constant__ CUtensorMap xmap,
                          const __grid_constant__ CUtensorMap dymap) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
-    uint64_t *full = (uint64_t *) (base + 2 * SW_STAGE);
+    uint8_t *dyb = base + 2 * SW_SLAB_MAX;   // SW_DYB buffers of SW_DY_MAX (1024-aligned)
+    uint64_t *full = (uint64_t *) (dyb + SW_DYB * SW_DY_MAX);
     uint64_t *empty = full + 2;
-    uint64_t *accum = empty + 2;
+    uint64_t *dy_full = empty + 2;
+    uint64_t *dy_empty = dy_full + SW_DYB;
+    uint64_t *accum = dy_empty + SW_DYB;
     uint32_t *tmem_holder = (uint32_t *) (accum + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
+        // two MMA issuers (warps 1 and 7) commit to every consumer barrier
         for (int s = 0; s < 2; s++) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], 2);
         }
-        tc::mbar_init(accum, 1);
+        for (int d = 0; d < SW_DYB; d++) {
+            tc::mbar_init(&dy_full[d], 1);
+            tc::mbar_init(&dy_empty[d], 2);
+        }
+        tc::mbar_init(accum, 2);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&xmap);
         tc::prefetch_tmap(&dymap);
@@ -87,54 +98,81 @@ __global__ void __launch_bounds__(192, 1)
     bool ok = true;
 
     if (warp == 0) {
-        // ------------------------------------------------ producer: slab rows and dY of each band
+        // ------------------------------------------------ producer: the slab rows of each band
         if (lane == 0) {
             for (int k = 0; k < nb; k++) {
                 const int s = k & 1;
                 if (k >= 2 && !(ok = tc::mbar_wait(&empty[s], ((k >> 1) + 1) & 1, p.err, 61))) break;
                 const int band = (int) blockIdx.x + k * (int) gridDim.x;
                 const int b = band / p.bands_per_img, oy0 = (band - b * p.bands_per_img) * SW_R;
-                const uint32_t st = tc::smem_u32(base + s * SW_STAGE);
+                const uint32_t st = tc::smem_u32(base + s * SW_SLAB_MAX);
                 tc::mbar_arrive_expect_tx(&full[s], p.tx);
-                for (int y = 0; y < SW_NY; y++)
+                for (int y = 0; y < p.nyl; y++)
 #pragma unroll
                     for (int sm = 0; sm < 2; sm++)
                         tc::tma_load_4d(st + (2 * y + sm) * p.pitch, &xmap, 0, p.col0[sm], 2 * oy0 - p.pad_h + y, b,
                                         &full[s]);
-                tc::tma_load_3d(st + SW_SLAB_MAX, &dymap, 0, 0, b * p.Ho + oy0, &full[s]);
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
-        // ------------------------------------------------ MMA issuer
+    } else if (warp == 6) {
+        // ------------------------------------------------ producer: dY, one output row per buffer
         if (lane == 0) {
+            int dq = 0;
+            for (int k = 0; k < nb && ok; k++) {
+                const int band = (int) blockIdx.x + k * (int) gridDim.x;
+                const int b = band / p.bands_per_img, oy0 = (band - b * p.bands_per_img) * SW_R;
+                const int rows = min(SW_R, p.Ho - oy0);
+                for (int r = 0; r < rows; r++, dq++) {
+                    const int d = dq % SW_DYB;
+                    if (dq >= SW_DYB && !(ok = tc::mbar_wait(&dy_empty[d], ((dq / SW_DYB) + 1) & 1, p.err, 64)))
+                        break;
+                    tc::mbar_arrive_expect_tx(&dy_full[d], (uint32_t) p.wpad * 128);
+                    tc::tma_load_3d(tc::smem_u32(dyb + d * SW_DY_MAX), &dymap, 0, 0, b * p.Ho + oy0 + r, &dy_full[d]);
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1 || warp == 7) {
+        // ------------------------------------------------ MMA issuers: warp 1 pairs 0-1, warp 7 pairs 2-3
+        // (one thread's loop overhead between MMAs would otherwise bound the issue rate)
+        if (lane == 0) {
+            const int m0 = warp == 1 ? 0 : 2;
             constexpr uint32_t idesc = tc::idesc_bf16(128, 64, 1, 1);
-            for (int k = 0; k < nb; k++) {
+            int dq = 0;
+            for (int k = 0; k < nb && ok; k++) {
                 const int s = k & 1;
                 if (!(ok = tc::mbar_wait(&full[s], (k >> 1) & 1, p.err, 62))) break;
                 tc::tc_fence_after();
                 const int band = (int) blockIdx.x + k * (int) gridDim.x;
                 const int b = band / p.bands_per_img, oy0 = (band - b * p.bands_per_img) * SW_R;
                 const int rows = min(SW_R, p.Ho - oy0);
-                const uint32_t sa = tc::smem_u32(base + s * SW_STAGE);
+                const uint32_t sa = tc::smem_u32(base + s * SW_SLAB_MAX);
                 // A: 16 core matrices one slab row apart, 8-pixel K groups 128 B apart;
-                // B: dY rows of 128 B, 128-byte swizzle, a 16-pixel K step is 2048 B
+                // B: a dY row of Wpad pixels x 128 B, 128-byte swizzle, a 16-pixel K step is 2048 B
                 const uint64_t a0 = tc::mn_interleave_desc(sa, 128, p.pitch);
-                const uint64_t b0 = tc::sw128_desc(sa + SW_SLAB_MAX, 8192, 1024);
-                for (int r = 0; r < rows; r++)
+                for (int r = 0; r < rows; r++, dq++) {
+                    const int d = dq % SW_DYB;
+                    if (!(ok = tc::mbar_wait(&dy_full[d], (dq / SW_DYB) & 1, p.err, 65))) break;
+                    tc::tc_fence_after();
+                    const uint64_t b0 = tc::sw128_desc(tc::smem_u32(dyb + d * SW_DY_MAX), 8192, 1024);
                     for (int ks = 0; ks < p.nks; ks++) {
-                        const uint64_t bd = b0 + (uint64_t) ((r * p.wpad * 128 + ks * 2048) >> 4);
+                        const uint64_t bd = b0 + (uint64_t) (ks * 128);
                         const uint64_t ar = a0 + (uint64_t) ((4 * r * p.pitch + 256 * ks) >> 4);
                         const uint32_t acc = (k | r | ks) != 0;
-                        for (int m = 0; m < p.npairs; m++)
-                            tc::mma_f16(tmem + (uint32_t) (64 * m), ar + (uint64_t) m, bd, idesc, acc);
+#pragma unroll
+                        for (int j = 0; j < 2; j++)
+                            if (m0 + j < p.npairs)
+                                tc::mma_f16(tmem + (uint32_t) (64 * (m0 + j)), ar + (uint64_t) (m0 + j), bd, idesc, acc);
                     }
+                    tc::mma_commit(&dy_empty[d]);
+                }
                 tc::mma_commit(&empty[s]);
             }
             tc::mma_commit(accum);
         }
         __syncwarp();
-    } else {
+    } else if (warp < 6) {
         // ------------------------------------------------ epilogue: the CTA's partial dW
         // D row L = 8 * (2 * ky + stream) + ci; pair m's columns 64m .. 64m + 63 are co
         if (ok) ok = tc::mbar_wait(accum, 0, p.err, 63);
@@ -187,7 +225,7 @@ bool stem_wgrad_geom(const cg_shape &s, StemWgGeom &sg) {
     sg.total_bands = s.b * sg.bands_per_img;
     const int sms = tc_num_sms();
     sg.grid = sg.total_bands < sms ? sg.total_bands : sms;
-    return 2 * sg.ent <= 256 && 2 * SW_NY * sg.pitch <= SW_SLAB_MAX && (uint32_t) SW_R * sg.wpad * 128 <= SW_DY_MAX;
+    return 2 * sg.ent <= 256 && 2 * SW_NY * sg.pitch <= SW_SLAB_MAX && (uint32_t) sg.wpad * 128 <= SW_DY_MAX;
 }
 
 }  // namespace
@@ -222,7 +260,8 @@ convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const voi
     p.col0[0] = 1 - s.hpad;
     p.col0[1] = -s.hpad;
     p.pitch = sg.pitch;
-    p.tx = 2 * SW_NY * (uint32_t) sg.ent * 16 + (uint32_t) SW_R * sg.wpad * 128;
+    p.nyl = 2 * (SW_R - 1) + s.kh;
+    p.tx = 2 * (uint32_t) p.nyl * sg.ent * 16;
     p.err = cg_device_error_word();
     if (!p.err) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
     CUtensorMap xmap, dymap;
@@ -234,10 +273,10 @@ convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const voi
         const unsigned estr[4] = {1, 2, 1, 1};
         if (convgemm_status_t e = tc_make_map_nd(&xmap, 4, x, dims, str, box, estr, 0)) return e;
     }
-    {   // dY [B*Ho][Wo][64]: box {64 channels, Wpad pixels, SW_R rows}, 128-byte swizzle
+    {   // dY [B*Ho][Wo][64]: box {64 channels, Wpad pixels, 1 row}, 128-byte swizzle
         const unsigned long long dims[3] = {64, (unsigned long long) g.wo, (unsigned long long) s.b * g.ho};
         const unsigned long long str[2] = {128, 128ull * g.wo};
-        const unsigned box[3] = {64, (unsigned) sg.wpad, (unsigned) SW_R};
+        const unsigned box[3] = {64, (unsigned) sg.wpad, 1};
         const unsigned estr[3] = {1, 1, 1};
         if (convgemm_status_t e = tc_make_map_nd(&dymap, 3, dy, dims, str, box, estr, 1)) return e;
     }
@@ -248,7 +287,7 @@ convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const voi
             return cg_cuda_check(e, "small-channel weight-gradient attribute");
         attr = true;
     }
-    if (convgemm_status_t e = cg_cuda_check(cg_launch_ex(CG_PDL_OFF, tc_stem_wgrad_kernel, dim3(sg.grid), dim3(192),
+    if (convgemm_status_t e = cg_cuda_check(cg_launch_ex(CG_PDL_OFF, tc_stem_wgrad_kernel, dim3(sg.grid), dim3(256),
                                                          SW_SMEM, st, p, xmap, dymap),
                                             "small-channel weight-gradient launch"))
         return e;
