@@ -56,7 +56,7 @@ struct StemWgParams {
     int *err;
 };
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(320, 1)
     tc_stem_wgrad_kernel(const __grid_constant__ StemWgParams p, const __grid_constant__ CUtensorMap xmap,
                          const __grid_constant__ CUtensorMap dymap) {
     extern __shared__ uint8_t smem_raw[];
@@ -71,16 +71,16 @@ __global__ void __launch_bounds__(256, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        // two MMA issuers (warps 1 and 7) commit to every consumer barrier
+        // one MMA issuer per tap pair (warps 1, 7, 8, 9) commits to every consumer barrier
         for (int s = 0; s < 2; s++) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 2);
+            tc::mbar_init(&empty[s], SW_MAXPAIRS);
         }
         for (int d = 0; d < SW_DYB; d++) {
             tc::mbar_init(&dy_full[d], 1);
-            tc::mbar_init(&dy_empty[d], 2);
+            tc::mbar_init(&dy_empty[d], SW_MAXPAIRS);
         }
-        tc::mbar_init(accum, 2);
+        tc::mbar_init(accum, SW_MAXPAIRS);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&xmap);
         tc::prefetch_tmap(&dymap);
@@ -133,11 +133,11 @@ __global__ void __launch_bounds__(256, 1)
             }
         }
         __syncwarp();
-    } else if (warp == 1 || warp == 7) {
-        // ------------------------------------------------ MMA issuers: warp 1 pairs 0-1, warp 7 pairs 2-3
-        // (one thread's loop overhead between MMAs would otherwise bound the issue rate)
+    } else if (warp == 1 || warp >= 7) {
+        // ------------------------------------------------ MMA issuers: one per tap pair, warp 1 pair 0,
+        // warps 7-9 pairs 1-3 (one thread's loop overhead between MMAs bounds its issue rate)
         if (lane == 0) {
-            const int m0 = warp == 1 ? 0 : 2;
+            const int m = warp == 1 ? 0 : warp - 6;
             constexpr uint32_t idesc = tc::idesc_bf16(128, 64, 1, 1);
             int dq = 0;
             for (int k = 0; k < nb && ok; k++) {
@@ -159,11 +159,8 @@ __global__ void __launch_bounds__(256, 1)
                     for (int ks = 0; ks < p.nks; ks++) {
                         const uint64_t bd = b0 + (uint64_t) (ks * 128);
                         const uint64_t ar = a0 + (uint64_t) ((4 * r * p.pitch + 256 * ks) >> 4);
-                        const uint32_t acc = (k | r | ks) != 0;
-#pragma unroll
-                        for (int j = 0; j < 2; j++)
-                            if (m0 + j < p.npairs)
-                                tc::mma_f16(tmem + (uint32_t) (64 * (m0 + j)), ar + (uint64_t) (m0 + j), bd, idesc, acc);
+                        if (m < p.npairs)
+                            tc::mma_f16(tmem + (uint32_t) (64 * m), ar + (uint64_t) m, bd, idesc, (k | r | ks) != 0);
                     }
                     tc::mma_commit(&dy_empty[d]);
                 }
@@ -287,7 +284,7 @@ convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const voi
             return cg_cuda_check(e, "small-channel weight-gradient attribute");
         attr = true;
     }
-    if (convgemm_status_t e = cg_cuda_check(cg_launch_ex(CG_PDL_OFF, tc_stem_wgrad_kernel, dim3(sg.grid), dim3(256),
+    if (convgemm_status_t e = cg_cuda_check(cg_launch_ex(CG_PDL_OFF, tc_stem_wgrad_kernel, dim3(sg.grid), dim3(320),
                                                          SW_SMEM, st, p, xmap, dymap),
                                             "small-channel weight-gradient launch"))
         return e;
