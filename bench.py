@@ -1178,7 +1178,7 @@ def main():
                             "gflop": fl / 1e9}
         del g_f
     kern_of = {"fwd": "tc_conv_kernel (forward)", "dgrad": "tc_conv_kernel (input gradient)",
-               "wgrad": "tc_wgrad_kernel + wgrad_reduce_kernel"}
+               "wgrad": "tc_wgrad_kernel + tc_stem_wgrad_kernel + wgrad_reduce_kernel"}
     dominant = max(("fwd", "dgrad", "wgrad"), key=lambda k: fam_summary[k]["ms"])
     dom = fam_summary[dominant]
     # algorithmic bytes of the family per step: X, dY (or W) read, output written once
@@ -1190,7 +1190,8 @@ def main():
         xb, yb = 2 * batch * l["h"] * l["w"] * c8(l["c"]), 2 * batch * ho * wo * l["kn"]
         wb = l["c"] * l["k"] * l["k"] * l["kn"]
         alg_bytes += xb + yb + wb * (4 if dominant == "wgrad" else 2)
-    traffic = profile_traffic(("tc_wgrad_kernel", "wgrad_reduce_kernel", "wgrad_group_sum_kernel")) \
+    traffic = profile_traffic(("tc_wgrad_kernel", "tc_stem_wgrad_kernel", "wgrad_reduce_kernel",
+                               "wgrad_group_sum_kernel")) \
         if dominant == "wgrad" else None
     roofline = {"bound": "tensor", "kernel": kern_of[dominant], "achieved": dom["tflops"],
                 "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",

@@ -10,16 +10,15 @@
 //   * a CTA takes bands of SW_R output rows of one image; for every input row of the band
 //     (2*(SW_R-1) + kh of them) and each of two column streams, one TMA load with traversal
 //     stride 2 brings the slab row
-//         S[2*y + st][s] = x[b][2*oy0 - pad_h + y][col0[st] + 2*s][0..7],  s < ent,
+//         S[2*y + st][s] = x[b][2*oy0 - pad_h + y][col0[st] + 2*s][0..7],  s < Wpad + npairs - 1,
 //     col0[0] = 1 - pad_w (taps kx = 2m+1), col0[1] = -pad_w (taps kx = 2m), so that tap
 //     pair m at output column ox reads entry s = ox + m of both streams;
 //   * for output row r of the band, the 16 core matrices (8 kernel rows x 2 streams,
 //     8 channels x 8 pixels each, no swizzle) of pair m start at slab row 4*r and are one
 //     slab row apart (SBO = the row pitch), 8-pixel K groups 128 bytes apart (LBO): one
 //     M=128 MMA per pair and 16-pixel K step, four TMEM accumulators of 64 columns;
-//   * a 16-byte TMA box row is one TMA element and the engine's element rate bounds these
-//     loads, so bands are tall (each input row is loaded by 2 of the band's 8 output rows'
-//     worth of work instead of 3.5) and slab stages are double-buffered across bands;
+//   * slab stages are double-buffered across bands; one MMA-issuing thread per tap pair
+//     (one thread's loop overhead between MMAs bounds its issue rate);
 //   * dY arrives per output row (64 channels x Wpad pixels, 128-byte swizzle, pixels past
 //     Wo zero-filled) through a ring of SW_DYB buffers filled by a second producer warp;
 //   * kernel rows >= kh (their slab rows are not loaded: stale data) and taps kx >= kw
