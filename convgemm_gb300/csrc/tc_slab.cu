@@ -58,15 +58,6 @@ struct SlabParams {
     uint32_t aoff[SLAB_MAXTAPS];  // byte offset of tap t's first row in a slab buffer
 };
 
-__device__ __forceinline__ void tma_load_4d_sw(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                               uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"((uint64_t) map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(tc::smem_u32(bar))
-        : "memory");
-}
-
 __device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, uint32_t src, int c0, int c1, int c2, int c3) {
     asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
                      (uint64_t) map),
@@ -141,7 +132,7 @@ __global__ void __launch_bounds__(288, 1)
                     const uint32_t ph = (it / p.nbuf) & 1;
                     if (it >= (uint32_t) p.nbuf && !(ok = tc::mbar_wait(&slab_free[s], ph ^ 1, p.err, 51))) break;
                     tc::mbar_arrive_expect_tx(&slab_full[s], p.slab_tx);
-                    tma_load_4d_sw(tc::smem_u32(slab + (size_t) s * p.buf_bytes), &xmap, cb * 64, ox0 + p.tx0,
+                    tc::tma_load_4d(tc::smem_u32(slab + (size_t) s * p.buf_bytes), &xmap, cb * 64, ox0 + p.tx0,
                                    oy0 + p.ty0, b, &slab_full[s]);
                 }
             }

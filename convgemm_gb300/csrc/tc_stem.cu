@@ -83,15 +83,6 @@ __device__ __forceinline__ uint64_t kmajor_desc(uint32_t saddr, uint32_t lead) {
     return d;
 }
 
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"((uint64_t) map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(tc::smem_u32(bar))
-        : "memory");
-}
-
 __device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int c0, int c1, int c2) {
     asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
                      (uint64_t) map),
@@ -189,7 +180,7 @@ __global__ void __launch_bounds__(288, 1)
                 const uint32_t dst = tc::smem_u32(slab + sb * p.buf_bytes);
                 tc::mbar_arrive_expect_tx(&slab_full[sb], p.slab_tx);
                 for (int rho = 0; rho < p.sw; rho++)
-                    tma_load_4d(dst + rho * p.rho_bytes, &xmap, 0, p.sw * (128 * wc + p.qmin) + rho,
+                    tc::tma_load_4d(dst + rho * p.rho_bytes, &xmap, 0, p.sw * (128 * wc + p.qmin) + rho,
                                 oy * p.sh - p.pad_h, b, &slab_full[sb]);
             }
         }
