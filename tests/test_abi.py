@@ -146,3 +146,31 @@ def test_batch_norm_training_entry_points_validate_without_gpu(cglib):
     assert L.convgemm_bn_stats_fold(0, 16, 10, None, None, 1e-5, 16, 16, None, None, None) == 1
     assert L.convgemm_bn_stats_fold(8, 16, 0, None, None, 1e-5, 16, 16, None, None, None) == 1
     assert L.convgemm_bn_apply_bf16(10, 12, 16, 16, 16, 1, 16, None) == 1     # kn % 8
+
+
+def test_stem_weight_gradient_plan_without_gpu(cglib):
+    """Weight-gradient planning needs no GPU. The ResNet-50 stem (c <= 8, stride 2, kn = 64) plans
+    one FP32 partial per CTA of its slab kernel (bands of 8 output rows, one CTA per SM), whatever
+    tile configuration is set. The workspace holds those partials plus the fixed-order reduction's
+    group sums (about eight partials per group once there are more than 16)."""
+    from convgemm_gb300 import tc
+    import torch
+    cg = cglib
+    s = cg.Shape.of(64, 224, 224, 3, 64, 7, 7, 3, 3, 2, 2)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 148
+    splits = min(sms, 64 * 14)
+    g = min(splits // 8, 32)
+    per = -(-splits // g)
+    groups = -(-splits // per)
+    try:
+        for bn, aux in ((0, 0), (128, 7), (64, 3 | tc.WGRAD_X_ON_A)):
+            if bn or aux:
+                tc.tune_set(tc.TUNE_WGRAD, s, bn, aux)
+            assert tc.wgrad_bf16_plan(s)[:2] == (64, splits)
+            assert tc.wgrad_bf16_workspace_size(s) == 4 * (splits + groups) * (49 * 8) * 64
+        # stride 1 (VGG's first layer) stays on the general kernel: its own split heuristic
+        v = cg.Shape.of(32, 224, 224, 3, 64, 3, 3, 1, 1, 1, 1)
+        tc.tune_set(tc.TUNE_WGRAD, v, 64, 5)
+        assert tc.wgrad_bf16_plan(v)[:2] == (64, 5)
+    finally:
+        tc.tune_clear()
