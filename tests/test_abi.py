@@ -174,3 +174,19 @@ def test_stem_weight_gradient_plan_without_gpu(cglib):
         assert tc.wgrad_bf16_plan(v)[:2] == (64, 5)
     finally:
         tc.tune_clear()
+
+
+def test_weight_gradient_flags_in_plan_without_gpu(cglib):
+    """The weight-gradient aux flags are parsed off the split count: X on the A side takes N tiles
+    of 64 / 128 / 256 output channels, and the split count in bits 0-15 still applies."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    s = cg.Shape.of(8, 14, 14, 256, 256, 3, 3, 1, 1, 1, 1)
+    try:
+        for bn, splits in ((128, 4), (256, 2), (64, 7)):
+            tc.tune_set(tc.TUNE_WGRAD, s, bn, splits | tc.WGRAD_X_ON_A)
+            assert tc.wgrad_bf16_plan(s)[:2] == (bn, splits)
+        tc.tune_set(tc.TUNE_WGRAD, s, 256, 3 | tc.WGRAD_IM2COL_X)
+        assert tc.wgrad_bf16_plan(s)[:2] == (256, 3)
+    finally:
+        tc.tune_clear()
