@@ -119,6 +119,7 @@ def lib():
         L.convgemm_set_pdl.argtypes = [_I]
         L.convgemm_set_pdl.restype = _I
         L.convgemm_dgrad_bf16_relu.argtypes = [SP, _VP, _VP, _VP, _VP, _VP]
+        L.convgemm_dgrad_bf16_ex.argtypes = [SP, _VP, _VP, _VP, _VP, _I, _VP]
         L.convgemm_selftest_wait_timeout.argtypes = [ctypes.c_uint, _VP]
         L.convgemm_bias_grad_bf16_workspace_size.argtypes = [SP]
         L.convgemm_bias_grad_bf16_workspace_size.restype = ctypes.c_size_t

@@ -2,8 +2,9 @@
 //
 // Each output element is one fused multiply-add chain per KC=384 block of the
 // reduction, blocks added in increasing order — the arithmetic of the
-// reference's loop nests with a BLIS micro-kernel (src/gemm_blis_B3A2C0_orig.c:
-// 216-264, betaI at :225; sxpbyM at src/gemm_blis.c:147-161), and the
+// reference's loop nests with a BLIS micro-kernel (the KC loop and betaI of
+// src/gemm_blis_B3A2C0_orig.c:55-64, src/gemm_blis_B3A2C0.c:64; sxpbyM at
+// src/gemm_blis.c:147-161), and the
 // reduction index runs in the reference's order k = (c*kh + kx)*kw + ky
 // (src/im2row_nhwc.c:163).  Forward and weight gradient therefore reproduce
 // the reference's values, not just its tolerance.

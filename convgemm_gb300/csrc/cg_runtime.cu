@@ -71,7 +71,12 @@ extern "C" void convgemm_clear_error(void) {
 }
 
 // ------------------------------------------------------- device error word
+// One word per device for every kernel of the library: a file-scope device
+// variable (zero when the module loads), so that no entry point allocates for it.
+// Host code cannot use the variable's name as a device address; its address on
+// the current device comes from cudaGetSymbolAddress, once per device.
 namespace {
+__device__ int g_dev_error_word;
 std::mutex g_err_mu;
 int *g_err_word[64] = {nullptr};
 }  // namespace
@@ -81,10 +86,9 @@ int *cg_device_error_word() {
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     std::lock_guard<std::mutex> lk(g_err_mu);
     if (!g_err_word[dev]) {
-        int *p = nullptr;
-        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
-        if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return nullptr;
-        g_err_word[dev] = p;
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_dev_error_word) != cudaSuccess) return nullptr;
+        g_err_word[dev] = (int *) p;
     }
     return g_err_word[dev];
 }

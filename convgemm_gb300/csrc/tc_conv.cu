@@ -12,15 +12,18 @@
 //   m = output pixel of the class (128 per tile),
 //   n = output channel (BN per tile, in TMEM columns),
 //   k = tap * Cin + ci over the class's taps (64 per pipeline stage).
-// A is gathered from the NHWC activation with 16-byte cp.async (zero-filled
-// for padding) straight into the 128-byte-swizzled K-major layout the tensor
-// core reads — no im2row buffer exists anywhere.  B is the packed weight
-// matrix [Cout][K] loaded by TMA.  The FP32 accumulator lives in TMEM.
+// A comes straight from the NHWC activation into the 128-byte-swizzled K-major
+// layout the tensor core reads: by im2col-mode TMA (128 pixels x 64 channels of
+// one tap per load, out-of-range taps zero-filled) when the channels come in
+// blocks of 64, else by 16-byte cp.async gathers, zero-filled for padding — no
+// im2row buffer exists anywhere.  B is the packed weight matrix [Cout][K]
+// loaded by TMA.  The FP32 accumulator lives in TMEM.
 //
 // The kernel is persistent: each CTA walks tiles blockIdx.x, +gridDim.x, ...
 // with two TMEM accumulators, so the epilogue of one tile runs while the MMAs
 // of the next accumulate.  Warp roles (288 threads):
-//   warps 0-3  gather A (thread 0 also issues the B TMA), stage ring of STAGES;
+//   warps 0-3  load A (one thread issuing the im2col TMA, or all four warps
+//              gathering), thread 0 also issues the B TMA; stage ring of STAGES;
 //   warps 4-7  epilogue: TMEM -> registers (tcgen05.ld), scale/shift/ReLU,
 //              BF16, then either a 128-byte-swizzled shared-memory tile and a
 //              TMA store (pixels contiguous in the output), or direct stores
@@ -413,6 +416,31 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                         if (col < p.Cout) {
                             part[col] = sum;
                             part[p.Cout + col] = sq;
+                        }
+                    }
+                }
+                if (!C::OUTF32 && p.accum && m < M && nb < p.Cout) {
+                    // accumulate (the reference's dx += ...): add the output's current 64 values in FP32
+                    size_t pix = (size_t) m;
+                    if (!p.epi_tma) {
+                        uint32_t q, jw, j, b;
+                        cl.dwg.divmod(m, q, jw);
+                        cl.dhg.divmod(q, b, j);
+                        pix = ((size_t) b * p.Hout + cl.oy0 + cl.osy * (int) j) * p.Wout + cl.ox0 + cl.osx * (int) jw;
+                    }
+                    const uint4 *orow4 = reinterpret_cast<const uint4 *>(p.out + pix * p.Cout + nb);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        uint4 ov = make_uint4(0, 0, 0, 0);
+                        if (nb + 8 * q + 8 <= p.Cout) ov = orow4[q];
+                        const uint32_t ow[4] = {ov.x, ov.y, ov.z, ov.w};
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const int jj = 8 * q + 2 * e;   // column of the low half
+                            uint32_t &lo = jj < 32 ? v0[jj] : v1[jj - 32];
+                            uint32_t &hi = jj + 1 < 32 ? v0[jj + 1] : v1[jj - 31];
+                            lo = __float_as_uint(__uint_as_float(lo) + __uint_as_float(ow[e] << 16));
+                            hi = __float_as_uint(__uint_as_float(hi) + __uint_as_float(ow[e] & 0xFFFF0000u));
                         }
                     }
                 }

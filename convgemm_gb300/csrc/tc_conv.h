@@ -35,6 +35,8 @@ struct TcConvParams {
     const float *shift;        // per output channel, or NULL
     int relu;
     const __nv_bfloat16 *mask;   // BF16 tensor laid out like out, or NULL: out = 0 where mask <= 0 (ReLU backward)
+    int accum;                 // BF16 input gradient: out = out + acc (the old value read first; FP32 sum, one
+                               // rounding), then the mask; 0: out overwritten
     float *stats;              // BF16 forward: per 32-row group g of the output pixels, [g][0][Cout] the sum
                                // and [g][1][Cout] the sum of squares of z = acc * scale + shift; or NULL
     int B, Hin, Win, Cin, Hout, Wout, Cout;

@@ -302,11 +302,11 @@ int tc_pick_bn(const TcPlan &pl, int sms) {
 convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, const void *wpacked, void *out,
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode,
                          const void *in_lo, const void *w_lo, int bn_override, int aux_override,
-                         const void *mask, float *stats) {
+                         const void *mask, float *stats, int accum) {
     if (pl.ncls == 0) return CONVGEMM_SUCCESS;
     // stride-1 layers with 64-channel blocks and several taps: operands from input slabs, unless the
     // tuning entry asks for the general kernel (aux bit 8)
-    if (mode == 0 && !mask && !stats && !(aux_override & 8) && tc_slab_applicable(pl) && !((uintptr_t) out & 15) &&
+    if (mode == 0 && !mask && !stats && !accum && !(aux_override & 8) && tc_slab_applicable(pl) && !((uintptr_t) out & 15) &&
         !((uintptr_t) in & 15) && !((uintptr_t) wpacked & 15))
         return tc_slab_run(pl, s, in, wpacked, out, scale, shift, relu, st);
     const int sms = tc_num_sms();
@@ -338,6 +338,7 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     p.shift = shift;
     p.relu = relu;
     p.mask = (const __nv_bfloat16 *) mask;
+    p.accum = accum;
     p.stats = stats;
     p.B = s.b;
     p.Hin = pl.Hin;
@@ -405,8 +406,7 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
 }
 
 // ------------------------------------------------------------ public API
-namespace {
-convgemm_status_t check_tc_shape(const convgemm_shape_t *shape, const char *fn) {
+convgemm_status_t tc_check_shape(const convgemm_shape_t *shape, const char *fn) {
     if (!shape) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: shape is NULL", fn);
     const convgemm_shape_t &s = *shape;
     if (s.b < 1 || s.h < 1 || s.w < 1 || s.c < 1 || s.kn < 1 || s.kh < 1 || s.kw < 1 || s.vstride < 1 ||
@@ -423,10 +423,9 @@ convgemm_status_t check_tc_shape(const convgemm_shape_t *shape, const char *fn) 
         return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: filters above 49 taps have no tensor-core kernel", fn);
     return CONVGEMM_SUCCESS;
 }
-}  // namespace
 
 extern "C" size_t convgemm_bf16_weights_size(const convgemm_shape_t *shape, int kind) {
-    if (check_tc_shape(shape, "convgemm_bf16_weights_size")) return 0;
+    if (tc_check_shape(shape, "convgemm_bf16_weights_size")) return 0;
     const cg_shape s = cg_from_public(*shape);
     TcPlan pl;
     if (kind == CONVGEMM_OPERAND_FWD) {
@@ -441,7 +440,7 @@ extern "C" size_t convgemm_bf16_weights_size(const convgemm_shape_t *shape, int 
 
 extern "C" convgemm_status_t convgemm_bf16_pack_weights(convgemm_layout_t layout, const convgemm_shape_t *shape,
                                                         int kind, const float *weights, void *packed, void *stream) {
-    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_bf16_pack_weights")) return e;
+    if (convgemm_status_t e = tc_check_shape(shape, "convgemm_bf16_pack_weights")) return e;
     if (!weights || !packed) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_bf16_pack_weights: NULL");
     const cg_shape s = cg_from_public(*shape);
     const int nchw = layout == CONVGEMM_NCHW;
@@ -485,7 +484,7 @@ extern "C" convgemm_status_t convgemm_to_bf16_nhwc(convgemm_layout_t layout, int
 extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, const void *x, const void *wpacked,
                                                void *y, const float *scale, const float *shift, int relu,
                                                void *stream) {
-    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_fwd_bf16")) return e;
+    if (convgemm_status_t e = tc_check_shape(shape, "convgemm_fwd_bf16")) return e;
     if (!x || !wpacked || !y) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_fwd_bf16: NULL tensor");
     if (shape->kn % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "convgemm_fwd_bf16: kn must be a multiple of 8");
     const cg_shape s = cg_from_public(*shape);
@@ -503,8 +502,8 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
 namespace {
 
 convgemm_status_t dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
-                             const void *mask, void *stream) {
-    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_dgrad_bf16")) return e;
+                             const void *mask, int accumulate, void *stream) {
+    if (convgemm_status_t e = tc_check_shape(shape, "convgemm_dgrad_bf16")) return e;
     if (!dy || !wpacked || !dx) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16: NULL tensor");
     if (shape->c % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "convgemm_dgrad_bf16: c must be a multiple of 8");
     const cg_shape s = cg_from_public(*shape);
@@ -512,29 +511,40 @@ convgemm_status_t dgrad_bf16(const convgemm_shape_t *shape, const void *dy, cons
     if (!tc_plan_dgrad(s, pl))
         return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "input gradient: more than 16 stride-phase classes");
     cudaStream_t st = (cudaStream_t) stream;
-    if (pl.has_empty_class) {
-        // pixels no tap reaches receive zero
+    if (pl.has_empty_class && !accumulate) {
+        // pixels no tap reaches receive zero (accumulating, they keep their value)
         if (convgemm_status_t e = cg_cuda_check(
                 cudaMemsetAsync(dx, 0, sizeof(__nv_bfloat16) * (size_t) s.b * s.h * s.w * s.c, st), "zero dx"))
             return e;
     }
     TcTune t{0, 0};
     tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
-    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits, mask);
+    if (accumulate && ((uintptr_t) dx & 15))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16_ex: accumulating dx not 16-byte aligned");
+    return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits, mask,
+                  nullptr, accumulate != 0);
 }
 
 }  // namespace
 
 extern "C" convgemm_status_t convgemm_dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
                                                  void *dx, void *stream) {
-    return dgrad_bf16(shape, dy, wpacked, dx, nullptr, stream);
+    return dgrad_bf16(shape, dy, wpacked, dx, nullptr, 0, stream);
 }
 
 extern "C" convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *shape, const void *dy,
                                                       const void *wpacked, void *dx, const void *x, void *stream) {
     if (!x || ((uintptr_t) x & 15))
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16_relu: x NULL or not 16-byte aligned");
-    return dgrad_bf16(shape, dy, wpacked, dx, x, stream);
+    return dgrad_bf16(shape, dy, wpacked, dx, x, 0, stream);
+}
+
+extern "C" convgemm_status_t convgemm_dgrad_bf16_ex(const convgemm_shape_t *shape, const void *dy,
+                                                    const void *wpacked, void *dx, const void *relu_x, int accumulate,
+                                                    void *stream) {
+    if (relu_x && ((uintptr_t) relu_x & 15))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16_ex: relu_x not 16-byte aligned");
+    return dgrad_bf16(shape, dy, wpacked, dx, relu_x, accumulate, stream);
 }
 
 // ------------------------------------------------------- weight gradient
@@ -609,7 +619,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
 
 extern "C" convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *shape, int *bn, int *splits,
                                                       int *max_splits) {
-    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_wgrad_bf16_plan")) return e;
+    if (convgemm_status_t e = tc_check_shape(shape, "convgemm_wgrad_bf16_plan")) return e;
     const WgPlan w = plan_wgrad(*shape);
     if (bn) *bn = w.bn;
     if (splits) *splits = w.splits;
@@ -618,14 +628,14 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *sh
 }
 
 extern "C" size_t convgemm_wgrad_bf16_workspace_size(const convgemm_shape_t *shape) {
-    if (check_tc_shape(shape, "convgemm_wgrad_bf16_workspace_size")) return 0;
+    if (tc_check_shape(shape, "convgemm_wgrad_bf16_workspace_size")) return 0;
     return plan_wgrad(*shape).ws_bytes;
 }
 
 extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_shape_t *shape,
                                                  const void *dy, const void *x, float *dw, void *workspace,
                                                  size_t workspace_bytes, void *stream) {
-    if (convgemm_status_t e = check_tc_shape(shape, "convgemm_wgrad_bf16")) return e;
+    if (convgemm_status_t e = tc_check_shape(shape, "convgemm_wgrad_bf16")) return e;
     if (!dy || !x || !dw || !workspace)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_wgrad_bf16: NULL tensor or workspace");
     if (layout != CONVGEMM_NHWC && layout != CONVGEMM_NCHW)
@@ -726,7 +736,7 @@ extern "C" convgemm_status_t convgemm_prep_prepare(int n, const convgemm_prep_it
     };
     for (int i = 0; i < n; i++) {
         const convgemm_prep_item_t &it = items[i];
-        if (convgemm_status_t e = check_tc_shape(&it.shape, fn)) return e;
+        if (convgemm_status_t e = tc_check_shape(&it.shape, fn)) return e;
         if (it.layout != CONVGEMM_NHWC && it.layout != CONVGEMM_NCHW)
             return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: item %d: bad layout", fn, i);
         if ((it.packed_fwd || it.packed_dgrad) && !it.weights)
@@ -816,7 +826,7 @@ extern "C" convgemm_status_t convgemm_prep_launch(const void *table, int njobs, 
 
 // ------------------------------------------------------------ bias gradient
 extern "C" size_t convgemm_bias_grad_bf16_workspace_size(const convgemm_shape_t *shape) {
-    if (check_tc_shape(shape, "convgemm_bias_grad_bf16_workspace_size")) return 0;
+    if (tc_check_shape(shape, "convgemm_bias_grad_bf16_workspace_size")) return 0;
     const ConvGeom g = make_geom(cg_from_public(*shape));
     return sizeof(float) * (size_t) tc_bias_grad_groups(g.P) * shape->kn;
 }
@@ -824,7 +834,7 @@ extern "C" size_t convgemm_bias_grad_bf16_workspace_size(const convgemm_shape_t 
 extern "C" convgemm_status_t convgemm_bias_grad_bf16(const convgemm_shape_t *shape, const void *dy, float *db,
                                                      void *workspace, size_t workspace_bytes, void *stream) {
     const char *fn = "convgemm_bias_grad_bf16";
-    if (convgemm_status_t e = check_tc_shape(shape, fn)) return e;
+    if (convgemm_status_t e = tc_check_shape(shape, fn)) return e;
     if (!dy || !db || !workspace) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL argument", fn);
     const size_t need = convgemm_bias_grad_bf16_workspace_size(shape);
     if (workspace_bytes < need)

@@ -45,6 +45,8 @@ convgemm_status_t tc_stem_run(const cg_shape &s, const void *x, const void *wpac
 int tc_stem_stat_groups(const cg_shape &s);
 
 int tc_num_sms();
+// Argument and size checks shared by the tensor-core entry points (records the error).
+convgemm_status_t tc_check_shape(const convgemm_shape_t *shape, const char *fn);
 // Weight gradient of stride-2 convolutions with c <= 8 and kn == 64 (the ResNet stem) from
 // input slabs: applicability, the number of FP32 partials (workspace planes before the
 // reduction's groups), and the run (partials into ws, then the fixed-order reduction into dw
@@ -66,4 +68,4 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
                          const float *scale, const float *shift, int relu, cudaStream_t st, int mode = 0,
                          const void *in_lo = nullptr, const void *w_lo = nullptr, int bn_override = 0,
                          int aux_override = 0, const void *mask = nullptr,
-                         float *stats = nullptr);
+                         float *stats = nullptr, int accum = 0);

@@ -1,12 +1,12 @@
 // Weight gradient (BF16 tensor cores) that allocates nothing.
 //
 // convgemm_wgrad_bf16 needs a caller workspace for its FP32 split partials.
-// Some callers cannot provide one or allocate at all: a framework that calls
-// the convolution from inside a CUDA-graph stream capture (cudaMalloc is not
-// allowed while a stream is being captured), and services that fix their GPU
-// memory footprint at start-up so that nothing can fail or fragment mid-run.
-// This entry point keeps the partials in a file-scope device array of fixed
-// size instead, so it calls no cudaMalloc/cudaFree and no allocating routine.
+// Some callers cannot provide one: code that runs while a stream is being
+// captured into a CUDA graph (cudaMalloc is not permitted during a capture), and
+// services that fix their GPU memory footprint at start-up so that nothing can
+// fail or fragment mid-run.  This entry point keeps the partials in a file-scope
+// device array of fixed size instead, so it calls no cudaMalloc/cudaFree and no
+// allocating routine.
 //
 // Limits and sharing:
 //   * the scratch holds CONVGEMM_NOALLOC_SCRATCH_FLOATS FP32 values (16 MiB);
@@ -19,6 +19,8 @@
 //     streams without ordering) race on it.  The array keeps the last call's
 //     partials; nothing in it needs to start at zero, because every element a
 //     call reads back was written by that call's kernel first.
+//   * a device-side wait that runs out is recorded in the library's device
+//     error word, like every other kernel's, and reported by convgemm_check_device;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) and sets kernel attributes; make that first call
 //     before any stream capture.
@@ -35,11 +37,10 @@
 namespace {
 
 static __device__ __align__(256) float g_wgrad_scratch[CONVGEMM_NOALLOC_SCRATCH_FLOATS];
-static __device__ int g_noalloc_wait_error;  // zero at load; set only by a timed-out device wait
 
 struct NoallocDevice {
     float *scratch = nullptr;
-    int *err = nullptr;
+    int *err = nullptr;   // the library's device error word (convgemm_check_device reads it)
     bool ready = false;
 };
 std::mutex g_noalloc_mu;
@@ -54,13 +55,13 @@ convgemm_status_t noalloc_setup(NoallocDevice **out) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoallocDevice &d = g_noalloc_dev[dev];
     if (!d.ready) {
-        void *p = nullptr, *q = nullptr;
+        void *p = nullptr;
         if (convgemm_status_t e = cg_cuda_check(cudaGetSymbolAddress(&p, g_wgrad_scratch), "cudaGetSymbolAddress"))
             return e;
-        if (convgemm_status_t e = cg_cuda_check(cudaGetSymbolAddress(&q, g_noalloc_wait_error), "cudaGetSymbolAddress"))
-            return e;
+        int *w = cg_device_error_word();
+        if (!w) return cg_set_error(CONVGEMM_ERROR_CUDA, "device error word unavailable");
         d.scratch = (float *) p;
-        d.err = (int *) q;
+        d.err = w;
         d.ready = true;
     }
     *out = &d;
@@ -77,18 +78,11 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
     if (!shape || !dy || !x || !dw) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL argument", fn);
     if (layout != CONVGEMM_NHWC && layout != CONVGEMM_NCHW)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: bad layout %d", fn, (int) layout);
-    const convgemm_shape_t &ps = *shape;
-    if (ps.b < 1 || ps.h < 1 || ps.w < 1 || ps.c < 1 || ps.kn < 1 || ps.kh < 1 || ps.kw < 1 || ps.vstride < 1 ||
-        ps.hstride < 1 || ps.vdil < 1 || ps.hdil < 1 || ps.vpad < 0 || ps.hpad < 0 ||
-        ps.h + 2LL * ps.vpad - (long long) ps.vdil * (ps.kh - 1) < 1 ||
-        ps.w + 2LL * ps.hpad - (long long) ps.hdil * (ps.kw - 1) < 1)
-        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: invalid geometry", fn);
-    const cg_shape s = cg_from_public(ps);
+    // the geometry, size and filter-size checks of the workspace form
+    if (convgemm_status_t e = tc_check_shape(shape, fn)) return e;
+    const cg_shape s = cg_from_public(*shape);
     const ConvGeom g = make_geom(s);
     const int Cp = rup(s.c, 8), kn8 = rup(s.kn, 8), Nx = s.kh * s.kw * Cp;
-    const long long lim = (1LL << 31) - 1;
-    if ((long long) s.b * s.h * s.w * Cp > lim || g.P * kn8 > lim)
-        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: a tensor has more than 2^31-1 elements", fn);
     const long long tile = (long long) Nx * s.kn;
     if (tile > (long long) CONVGEMM_NOALLOC_SCRATCH_FLOATS)
         return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED,
@@ -105,7 +99,9 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layou
     const int mtiles = (Mext + 127) / 128, ntiles = (Next + bn - 1) / bn;
     const int nchunks = (int) ((g.P + 63) / 64);
     const int base = mtiles * ntiles;
-    int splits = (152 * (bn == 256 ? 1 : 2) + base - 1) / base;
+    // the workspace form's default: one wave of CTAs (no partial second wave), at least 8
+    // chunks (512 pixels) per split
+    int splits = tc_num_sms() * (bn == 256 ? 1 : 2) / base;
     splits = splits > (nchunks + 7) / 8 ? (nchunks + 7) / 8 : splits;
     const int fit = (int) ((long long) CONVGEMM_NOALLOC_SCRATCH_FLOATS / tile);
     if (splits > fit) splits = fit;

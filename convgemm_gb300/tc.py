@@ -50,6 +50,12 @@ def dgrad_bf16_relu(shape: Shape, dy, wpacked, dx, x, stream=None):
                                              _stream(stream)))
 
 
+def dgrad_bf16_ex(shape: Shape, dy, wpacked, dx, relu_x=None, accumulate=False, stream=None):
+    """Input gradient; accumulate=True adds into dx (the reference's dx += ...), relu_x masks the result."""
+    _raise_if(lib().convgemm_dgrad_bf16_ex(ctypes.byref(shape), ptr(dy), ptr(wpacked), ptr(dx), ptr(relu_x),
+                                           int(bool(accumulate)), _stream(stream)))
+
+
 def bias_grad_bf16(shape: Shape, dy, db, workspace=None, stream=None):
     """db[co] = sum over output pixels of dy[p][co] (FP32, fixed order)."""
     import torch

@@ -78,7 +78,9 @@ int convgemm_set_pdl(int on);
 const char *convgemm_get_last_error(void);
 void convgemm_clear_error(void);
 /* Reads (and clears) the device-side error word that bounded waits set; it
- * synchronises the stream first. */
+ * synchronises the stream first.  One word per device serves every kernel of the
+ * library, convgemm_wgrad_bf16_noalloc's included; it is a file-scope device
+ * variable, so neither this call nor any kernel launch allocates for it. */
 convgemm_status_t convgemm_check_device(void *stream);
 
 /* ------------------------------------------------------- FP32 plain form */
@@ -281,6 +283,15 @@ convgemm_status_t convgemm_wgrad_bf16_plan(const convgemm_shape_t *shape, int *b
 convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
                                            const void *x, void *stream);
 
+/* Input gradient with the reference's accumulate semantics: sconvGemmNHWC_back
+ * adds into dx (beta = 1, src/convGemm.c:94-95; NCHW twin 142-143).  accumulate != 0:
+ * dx = dx + dgrad(dy, w), the old BF16 value read in the epilogue and added in FP32
+ * before one rounding; accumulate == 0: dx overwritten, as convgemm_dgrad_bf16.
+ * relu_x (optional, as for convgemm_dgrad_bf16_relu): the result is then zeroed
+ * where relu_x <= 0, after the sum.  dx must be 16-byte aligned when accumulating. */
+convgemm_status_t convgemm_dgrad_bf16_ex(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
+                                         const void *relu_x, int accumulate, void *stream);
+
 /* Bias gradient of the convolution: db[co] = sum over the b*ho*wo output pixels of
  * dy[p][co] (dy BF16 NHWC with kn rounded up to 8 channels, as for
  * convgemm_wgrad_bf16), FP32 in a fixed order (bit-reproducible). */
@@ -331,7 +342,9 @@ convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const convgemm_s
  * values) that every GPU loading the library keeps until exit; layers with
  * kh*kw*c8*kn above that are rejected with CONVGEMM_ERROR_NOT_SUPPORTED.  All
  * calls share the array, so calls that overlap on the GPU race.  The first call
- * on a device looks up the array's address; make it before any stream capture. */
+ * on a device looks up the array's address; make it before any stream capture.
+ * The same shape checks as convgemm_wgrad_bf16 apply (filters up to 49 taps); a
+ * device-side wait that runs out is reported by convgemm_check_device. */
 convgemm_status_t convgemm_wgrad_bf16_noalloc(convgemm_layout_t layout, const convgemm_shape_t *shape,
                                               const void *dy, const void *x, float *dw, void *stream);
 

@@ -5,13 +5,13 @@
  * TEST INFRASTRUCTURE ONLY: tests/ use it as a checker and bench.py times it as
  * the CPU baseline on hosts where the reference's sources are not present.
  *
- * What "the reference's order" means (src/gemm_blis_B3A2C0_orig.c:216-264,
- * src/gemm_blis_B3A2C0.c:329-381): the reduction dimension is cut into blocks
+ * What "the reference's order" means (src/gemm_blis_B3A2C0_orig.c:55-64,
+ * src/gemm_blis_B3A2C0.c:58-64): the reduction dimension is cut into blocks
  * of KC = 384 (slides/slides.tex:158-160); each block is one fused
  * multiply-add chain per output element, in increasing k, starting from +0
  * (the BLIS micro-kernel, gemm_blis.h:65-76); blocks are added to the running
  * result in increasing order (betaI = beta on the first block and 1 after,
- * B3A2C0_orig.c:225; sxpbyM, gemm_blis.c:147-161).  The epilogue runs on the
+ * B3A2C0_orig.c:64; sxpbyM, gemm_blis.c:147-161).  The epilogue runs on the
  * last block only: t = block + running (if any), t += bias,
  * t = (t - mean)*inv_std, t = t*gamma + beta (fused, as gcc contracts it at
  * -Ofast), ReLU (src/im2row_nhwc.c:269-285, src/im2col_nchw.c:419-432).
@@ -292,4 +292,73 @@ void port_sconvGemmNCHW_back(int b, int c, int h, int w, int kn, int kh, int kw,
     float *dyt = nchw_to_pk(&d, dy);
     dgrad_core(&d, 1, weights, dyt, dx);   /* OIHW weights are already [kn][K] */
     free(dyt);
+}
+
+/* ---- sampled points of the port, in the same per-element arithmetic ----
+ * For layers too large to restate whole in a test: out[i] is the port's value of
+ * output element idx[i] (the forward's y, or the weight gradient's dW, indexed as
+ * the reference lays them out for `layout`), computed with the same KC = 384
+ * blocked FMA chains, block sums and epilogue as fwd_core / wgrad_core above, so
+ * each equals the corresponding element of port_sconvGemm{NHWC,NCHW} bit for bit.
+ * Weights are in the reference layout of `layout` ([c][kh][kw][kn] / [kn][c][kh][kw]);
+ * dy is NHWC [b][ho][wo][kn] or NCHW [b][kn][ho][wo]. */
+void port_fwd_points(int layout, int b, int h, int w, int c, int kn, int kh, int kw, int vpad, int hpad,
+                     int vstr, int hstr, int vdil, int hdil, const float *wts, const float *x,
+                     const int64_t *idx, int64_t n, float *out, const float *bias, const float *mean,
+                     const float *inv_std, const float *gamma, const float *beta, int relu) {
+    pdesc d = mkdesc(b, h, w, c, kn, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil);
+    const int nchw = layout == 1;
+    const int K = c * kh * kw;
+    pepi e = {bias, mean, inv_std, gamma, beta, relu != 0, nchw || bias != NULL || mean != NULL || relu};
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; i++) {
+        int64_t o = idx[i];
+        int bb, ox, oy, co;
+        if (nchw) {
+            oy = (int) (o % d.wo); ox = (int) ((o / d.wo) % d.ho);
+            co = (int) ((o / ((int64_t) d.wo * d.ho)) % kn); bb = (int) (o / ((int64_t) d.wo * d.ho * kn));
+        } else {
+            co = (int) (o % kn); oy = (int) ((o / kn) % d.wo);
+            ox = (int) ((o / ((int64_t) kn * d.wo)) % d.ho); bb = (int) (o / ((int64_t) kn * d.wo * d.ho));
+        }
+        float S = 0.0f;
+        for (int pc = 0; pc < K; pc += CG_KC) {
+            int kc = (K - pc < CG_KC) ? K - pc : CG_KC;
+            float blk = 0.0f;
+            for (int k = pc; k < pc + kc; k++) {
+                const float wv = nchw ? wts[(size_t) co * K + k] : wts[(size_t) k * kn + co];
+                blk = fmaf(xval(&d, nchw, x, bb, ox, oy, k), wv, blk);
+            }
+            S = (pc == 0) ? blk : blk + S;
+        }
+        out[i] = e.any ? epilogue(S, co, &e) : S;
+    }
+}
+
+void port_wgrad_points(int layout, int b, int h, int w, int c, int kn, int kh, int kw, int vpad, int hpad,
+                       int vstr, int hstr, int vdil, int hdil, const float *dy, const float *x,
+                       const int64_t *idx, int64_t n, float *out) {
+    pdesc d = mkdesc(b, h, w, c, kn, kh, kw, vpad, hpad, vstr, hstr, vdil, hdil);
+    const int nchw = layout == 1;
+    const int K = c * kh * kw;
+    const int64_t P = (int64_t) d.b * d.ho * d.wo, hw = (int64_t) d.ho * d.wo;
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t i = 0; i < n; i++) {
+        const int64_t o = idx[i];
+        const int k = nchw ? (int) (o % K) : (int) (o / kn);
+        const int co = nchw ? (int) (o / K) : (int) (o % kn);
+        float S = 0.0f;
+        for (int64_t pc = 0; pc < P; pc += CG_KC) {
+            int64_t kc = (P - pc < CG_KC) ? P - pc : CG_KC;
+            float blk = 0.0f;
+            for (int64_t p = pc; p < pc + kc; p++) {
+                int oy = (int) (p % d.wo), ox = (int) ((p / d.wo) % d.ho), bb = (int) (p / hw);
+                const float dv = nchw ? dy[((int64_t) bb * kn + co) * hw + (int64_t) ox * d.wo + oy]
+                                      : dy[(size_t) p * kn + co];
+                blk = fmaf(dv, xval(&d, nchw, x, bb, ox, oy, k), blk);
+            }
+            S = (pc == 0) ? blk : S + blk;
+        }
+        out[i] = S;
+    }
 }

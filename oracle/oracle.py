@@ -26,7 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libconvgemm_ref.so")
-REF_SRC = "/root/reference/src"
+REF_SRC = os.path.join(os.environ.get("CONVGEMM_REFERENCE", "/root/reference"), "src")
 
 NHWC, NCHW = 0, 1
 
@@ -84,6 +84,8 @@ def lib():
         L.oracle_bn_fold_f64.argtypes = [_I, _FP, _FP, _FP, _FP, _FP, _DP, _DP]
         L.oracle_im2row_nhwc.argtypes = [_FP, _FP] + [_I] * 12
         L.oracle_im2col_nchw.argtypes = [_FP, _FP] + [_I] * 12
+        L.port_fwd_points.argtypes = [_I] * 14 + [_FP, _FP, _LP, ctypes.c_int64, _FP, _FP, _FP, _FP, _FP, _FP, _I]
+        L.port_wgrad_points.argtypes = [_I] * 14 + [_FP, _FP, _LP, ctypes.c_int64, _FP]
         for name in ("port_sconvGemmNHWC", "port_sconvGemmNCHW"):
             getattr(L, name).argtypes = _API_FWD
         for name in ("port_sconvGemmNHWC_back", "port_sconvGemmNCHW_back"):
@@ -168,6 +170,25 @@ def dgrad_points_f64(layout, g, wts, dy, idx):
     idx = np.ascontiguousarray(idx, dtype=np.int64)
     out = np.empty(idx.shape[0], np.float64)
     lib().oracle_dgrad_points_f64(layout, *_geom(g), _f32p(wts), _f32p(dy), _i64p(idx), idx.shape[0], _f64p(out))
+    return out
+
+
+def port_fwd_points(layout, g, wts, x, idx, epi=None):
+    """The FP32 port's forward at sampled output indices (bit-identical to the whole-layer port)."""
+    epi = epi or {}
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.empty(idx.shape[0], np.float32)
+    lib().port_fwd_points(layout, *_geom(g), _f32p(wts), _f32p(x), _i64p(idx), idx.shape[0], _f32p(out),
+                          _f32p(epi.get("bias")), _f32p(epi.get("mean")), _f32p(epi.get("inv_std")),
+                          _f32p(epi.get("gamma")), _f32p(epi.get("beta")), int(bool(epi.get("relu", False))))
+    return out
+
+
+def port_wgrad_points(layout, g, dy, x, idx):
+    """The FP32 port's weight gradient at sampled dW indices (bit-identical to the whole-layer port)."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.empty(idx.shape[0], np.float32)
+    lib().port_wgrad_points(layout, *_geom(g), _f32p(dy), _f32p(x), _i64p(idx), idx.shape[0], _f32p(out))
     return out
 
 

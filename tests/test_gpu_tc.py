@@ -406,6 +406,55 @@ def test_dgrad_relu_mask_fused(cglib, shape):
     assert torch.equal(dxm.view(torch.int16), want.view(torch.int16))
 
 
+ACC_SHAPES = [(2, 14, 14, 64, 64, 3, 1, 1, 1),    # stride 1, 64 channels (otherwise the slab kernel's shape)
+              (2, 14, 14, 256, 512, 1, 0, 2, 1),  # 1x1/s2: three classes receive no tap and keep dx
+              (2, 9, 9, 128, 64, 3, 1, 2, 1),     # four stride-phase classes, direct stores
+              (1, 12, 10, 32, 48, 3, 2, 1, 2)]    # ragged channels: cp.async gather path
+
+
+@pytest.mark.parametrize("shape", ACC_SHAPES, ids=str)
+@pytest.mark.parametrize("masked", [False, True], ids=["plain", "relu"])
+def test_dgrad_bf16_accumulates_like_the_reference(cglib, oracle_lib, shape, masked):
+    """accumulate=1 adds the input gradient into dx (sconvGemmNHWC_back's dx += ..., src/convGemm.c:94-95):
+    FP64 oracle of dx0 + dgrad on the same BF16 inputs, within the BF16 output tolerance; with the ReLU
+    mask the sum is zeroed where x <= 0."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, stride=stride, dil=dil)
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(31 + sum(shape))
+    K = c * k * k
+    wt = (rng.standard_normal(K * kn) * np.sqrt(2.0 / K)).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    wp = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    dx0 = torch.from_numpy(rng.standard_normal(b * h * w * c).astype(np.float32)).cuda().to(torch.bfloat16)
+    dx0 = dx0.reshape(b, h, w, c)
+    x = None
+    if masked:
+        x = (torch.rand(b, h, w, c, device="cuda") - 0.3).to(torch.bfloat16)
+    dx = dx0.clone()
+    tc.dgrad_bf16_ex(s, dyd, wp, dx, relu_x=x, accumulate=True)
+    torch.cuda.synchronize()
+    cg.check_device()
+    want = dx0.double().cpu().numpy().ravel() + O.dgrad_f64(C.NHWC, g, bf16r(wt), bf16r(dy))
+    if masked:
+        want = np.where(x.float().cpu().numpy().ravel() > 0, want, 0.0)
+    got = dx.float().cpu().numpy().ravel()
+    assert rel_max_rms(got, want)[0] <= BF16_SELF_TOL
+    # accumulate = 0 through the same entry point is the overwriting input gradient, bit for bit
+    over = torch.full_like(dx, float("nan"))
+    tc.dgrad_bf16_ex(s, dyd, wp, over, relu_x=x, accumulate=False)
+    ref_over = torch.empty_like(dx)
+    if masked:
+        tc.dgrad_bf16_relu(s, dyd, wp, ref_over, x)
+    else:
+        tc.dgrad_bf16(s, dyd, wp, ref_over)
+    torch.cuda.synchronize()
+    assert torch.equal(over.view(torch.int16), ref_over.view(torch.int16))
+
+
 @pytest.mark.parametrize("shape", [(2, 14, 14, 64, 96, 3, 1, 1, 1), (8, 28, 28, 64, 256, 1, 0, 1, 1)], ids=str)
 def test_bias_grad_against_fp64(cglib, shape):
     """db = sum over output pixels of dY: within FP32 rounding of FP64, and reproducible."""

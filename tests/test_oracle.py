@@ -128,7 +128,8 @@ def test_bn_fold(oracle_lib):
     assert np.allclose(v * scale + shift, want, rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference checkout not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("CONVGEMM_REFERENCE", "/root/reference"), "src")),
+                    reason="reference checkout not present")
 def test_port_matches_reference_random_shapes(oracle_lib):
     """Restatement vs the reference's own code on shapes outside the fixtures."""
     O = oracle_lib
@@ -157,3 +158,22 @@ def test_port_matches_reference_random_shapes(oracle_lib):
             O.call_fwd("ref", layout, g, dy, x, a, trans="T")
             O.call_fwd("port", layout, g, dy, x, b, trans="T")
             assert bitexact(a, b)
+
+
+@pytest.mark.parametrize("name", ["config1_fwd_nhwc", "fwd_nchw_bias_relu_s2", "fwd_nhwc_bias_k432",
+                                  "wgrad_nhwc_3x3", "wgrad_nchw_1x1_s2", "wgrad_nhwc_s2_p1000"])
+def test_port_sampled_points_equal_the_whole_layer_port(oracle_lib, name):
+    """The port's sampled-point functions (used at full ResNet-50 size on the GPU machine) give the
+    whole-layer port's values bit for bit, so a sampled FP32 check is as strict as a whole one."""
+    O = oracle_lib
+    case = next(c for c in C.CASES if c[0] == name)
+    _, op, layout, g, _, _ = case
+    inp = C.make_inputs(*case)
+    n_out = load(name)["out"].size
+    whole = port_result(O, op, layout, g, inp, n_out)
+    idx = np.random.default_rng(5).choice(n_out, size=min(n_out, 500), replace=False)
+    if op == "fwd":
+        pts = O.port_fwd_points(layout, g, inp["w"], inp["x"], idx, inp["epi"])
+    else:
+        pts = O.port_wgrad_points(layout, g, inp["dy"], inp["x"], idx)
+    assert np.array_equal(pts.view(np.int32), np.asarray(whole, np.float32)[idx].view(np.int32))
