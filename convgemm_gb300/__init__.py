@@ -149,6 +149,11 @@ def lib():
         L.convgemm_group_table_size.restype = ctypes.c_size_t
         L.convgemm_group_prepare.argtypes = [_I, _VP, _VP, ctypes.c_size_t, ctypes.POINTER(_I)]
         L.convgemm_group_launch.argtypes = [_VP, _I, _I, _VP]
+        L.convgemm_weights_cached.argtypes = [_I, SP, _I, _VP, ctypes.c_ulonglong, ctypes.POINTER(_VP),
+                                              ctypes.POINTER(_VP), _VP]
+        L.convgemm_weights_cache_evict.argtypes = [_VP]
+        L.convgemm_weights_cache_evict.restype = _I
+        L.convgemm_weights_cache_bytes.restype = ctypes.c_size_t
         _lib = L
     return _lib
 
@@ -229,6 +234,8 @@ def ptr(t):
     """Address of a numpy array or torch tensor (None -> NULL)."""
     if t is None:
         return None
+    if isinstance(t, int):   # a device address returned by the library (e.g. a cached operand)
+        return t
     if hasattr(t, "data_ptr"):
         if not t.is_contiguous():
             raise ValueError("tensor must be contiguous")

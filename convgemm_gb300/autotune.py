@@ -29,7 +29,8 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
-OP_CACHE_TAG = "v5"   # op entries: fwd / dgrad with the M-tile and epilogue-warp choices; wgrad with 2-chunk stages, direct single-split writes and 2..8-split clusters
+OP_CACHE_TAG = "v5"   # op entries: fwd / dgrad with the M-tile and epilogue-warp choices
+WGRAD_CACHE_TAG = "v6"   # wgrad: 2-chunk stages, direct single-split writes, 2..8-split clusters, grouped clusters
 
 
 def cache_path() -> str:
@@ -146,7 +147,8 @@ OP_NAMES = {tc.TUNE_FWD: "fwd", tc.TUNE_DGRAD: "dgrad", tc.TUNE_WGRAD: "wgrad", 
 
 
 def op_key(op: int, s) -> str:
-    return f"{OP_NAMES[op]}.{OP_CACHE_TAG}|{shape_key(s)}"
+    tag = WGRAD_CACHE_TAG if op == tc.TUNE_WGRAD else OP_CACHE_TAG
+    return f"{OP_NAMES[op]}.{tag}|{shape_key(s)}"
 
 
 def graph_time_us(run, reps: int = 10) -> float:
@@ -209,6 +211,8 @@ def op_candidates(op: int, s):
                 for sp in sorted({max(1, s2 // 2), s2, min(mx, 2 * s2)} | {x for x in (2, 4, 8) if x <= mx}):
                     out.append((w, sp | tc.WGRAD_X_ON_A))
             tc.tune_set(op, s, 0, 0)
+    # more than 8 splits: also the in-kernel reduction by clusters of 2 / 4 / 8 splits
+    out += [(w, sp | tc.WGRAD_GROUPS(cs)) for w, sp in list(out) if (sp & 0xffff) > 8 for cs in (2, 4, 8)]
     return out
 
 

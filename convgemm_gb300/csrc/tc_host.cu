@@ -501,6 +501,27 @@ extern "C" convgemm_status_t convgemm_fwd_bf16(const convgemm_shape_t *shape, co
 
 namespace {
 
+// dx = 0 where x <= 0, 8 BF16 values per thread (n8 groups of 8): applied before an accumulating,
+// masked input gradient whose stride-phase classes do not reach every pixel, so that the pixels
+// no tap reaches (which the kernel leaves alone) carry the mask too.
+__global__ void relu_mask_bf16_kernel(uint4 *__restrict__ dx, const uint4 *__restrict__ x, size_t n8) {
+    for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n8; i += (size_t) gridDim.x * blockDim.x) {
+        uint4 d = dx[i];
+        const uint4 v = x[i];
+        uint32_t *dw = &d.x;
+        const uint32_t *xw = &v.x;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const __nv_bfloat162 xv = *reinterpret_cast<const __nv_bfloat162 *>(&xw[j]);
+            uint32_t keep = 0;
+            if (__bfloat162float(xv.x) > 0.0f) keep |= 0x0000ffffu;
+            if (__bfloat162float(xv.y) > 0.0f) keep |= 0xffff0000u;
+            dw[j] &= keep;
+        }
+        dx[i] = d;
+    }
+}
+
 convgemm_status_t dgrad_bf16(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
                              const void *mask, int accumulate, void *stream) {
     if (convgemm_status_t e = tc_check_shape(shape, "convgemm_dgrad_bf16")) return e;
@@ -521,6 +542,14 @@ convgemm_status_t dgrad_bf16(const convgemm_shape_t *shape, const void *dy, cons
     tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
     if (accumulate && ((uintptr_t) dx & 15))
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "convgemm_dgrad_bf16_ex: accumulating dx not 16-byte aligned");
+    if (pl.has_empty_class && accumulate && mask) {
+        // the pixels no tap reaches keep dx, masked like every other pixel
+        const size_t n8 = (size_t) s.b * s.h * s.w * s.c / 8;
+        const int blocks = (int) ((n8 + 255) / 256 < 4096 ? (n8 + 255) / 256 : 4096);
+        relu_mask_bf16_kernel<<<blocks, 256, 0, st>>>((uint4 *) dx, (const uint4 *) mask, n8);
+        cg_note_launch();
+        if (convgemm_status_t e = cg_cuda_check(cudaGetLastError(), "relu mask of dx")) return e;
+    }
     return tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn, t.splits, mask,
                   nullptr, accumulate != 0);
 }
@@ -554,6 +583,7 @@ namespace {
 
 struct WgPlan {
     int xa, bn, x2d, stem, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
+    int csize, groups;   // grouped cluster reduction (groups > 1): splits = groups * csize
     size_t ws_bytes;
 };
 
@@ -612,6 +642,27 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         w.splits = tc_stem_wgrad_splits(s);
     }
     w.ws_bytes = sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
+    // more splits than one cluster: clusters of up to 8 splits, reduced in the kernel (the
+    // workspace is sized for the smallest cluster, so that it does not depend on the device)
+    w.csize = w.groups = 0;
+    if (!w.stem && w.splits > 8) {
+        const size_t tile_bytes = sizeof(float) * 128 * (size_t) w.bn * (size_t) w.mtiles * (size_t) w.ntiles;
+        const size_t grouped = tile_bytes * (size_t) ((w.splits + 1) / 2);
+        if (grouped > w.ws_bytes) w.ws_bytes = grouped;
+        const int code = (t.splits >> 20) & 3;   // CONVGEMM_WGRAD_GROUPS: 1, 2, 3 -> clusters of 2, 4, 8
+        const int want = code ? 1 << code : 0;
+        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want) ? want : 0;
+        if (cs) {
+            w.csize = cs;
+            w.groups = (w.splits + cs - 1) / cs;
+            w.splits = w.groups * cs;
+            w.cps = (w.nchunks + w.splits - 1) / w.splits;
+            // a workspace that is not 16-byte aligned takes the reduction kernels at this split count
+            const size_t planes =
+                sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
+            if (planes > w.ws_bytes) w.ws_bytes = planes;
+        }
+    }
     return w;
 }
 
@@ -698,7 +749,17 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.direct = w.splits == 1;
     p.layout = layout == CONVGEMM_NCHW;
     p.C = s.c;
-    p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits);
+    if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
+        // clusters of csize splits; the tile's last cluster adds the clusters' sums
+        p.cluster = 1;
+        p.groups = w.groups;
+        p.csize = w.csize;
+        p.gws = (float *) workspace;
+        p.counters = tc_wgrad_counters(w.mtiles * w.ntiles * w.csize);
+        if (!p.counters) return cg_set_error(CONVGEMM_ERROR_CUDA, "convgemm_wgrad_bf16: tile counters unavailable");
+    } else {
+        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits);
+    }
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
         return e;

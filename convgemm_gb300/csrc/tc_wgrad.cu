@@ -22,6 +22,8 @@
 // tile shape and traffic).
 #include <cuda_bf16.h>
 
+#include <mutex>
+
 #include "cg_common.cuh"
 #include "tc_ptx.cuh"
 #include "tc_wgrad.h"
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t v[32];
-                if (ok) {
+                if (ok && KT > 0) {   // a split past the last chunk (grouped clusters) adds zero
                     tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
                     tc::tmem_ld_wait();
                 } else {
@@ -315,7 +317,9 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
 
     if (p.cluster) {
         // dW = sum of the cluster's partial tiles in split (cluster rank) order; rank r adds rows
-        // [r*rows, (r+1)*rows) across all ranks' shared memory and writes them
+        // [r*rows, (r+1)*rows) across all ranks' shared memory and writes them.  With grouped
+        // clusters (p.groups > 1) the slice goes to gws instead, and the last cluster of the
+        // tile to arrive adds the groups' slices in group order and writes dW.
         asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
         if (warp < 4) {
             uint32_t rank, nrank;
@@ -325,28 +329,15 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
             const int nr = min(rows, 128 - r0);
             const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx, khw = p.kh * p.kw;
             const uint32_t Rloc = tc::smem_u32(base);
+            const int G = p.groups > 1 ? p.groups : 1;
+            const int tile = blockIdx.x + gridDim.x * blockIdx.y;
+            // this cluster's slice of the tile in gws: [tile][group][128][BN]
+            float *gslice = G > 1 ? p.gws + ((size_t) (tile * G + (int) (blockIdx.z / nrank)) * 128) * BN : nullptr;
             // lanes along rows when rows are dW's contiguous index (co, NHWC layout), else along columns
             const bool row_fast = !XA && p.layout == 0;
-            for (int e = threadIdx.x; e < nr * (BN / 4); e += 128) {
-                const int rr = row_fast ? e % nr : e / (BN / 4), c4 = row_fast ? e / nr : e % (BN / 4);
-                const int row = r0 + rr;
-                const uint32_t off = (uint32_t) ((row * (BN + 4) + 4 * c4) * 4);
-                float a[4] = {0.f, 0.f, 0.f, 0.f};
-                for (uint32_t z = 0; z < nrank; z++) {
-                    uint32_t ra;
-                    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(Rloc + off), "r"(z));
-                    float b0, b1, b2, b3;
-                    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-                                 : "=f"(b0), "=f"(b1), "=f"(b2), "=f"(b3)
-                                 : "r"(ra)
-                                 : "memory");
-                    a[0] = __fadd_rn(a[0], b0);
-                    a[1] = __fadd_rn(a[1], b1);
-                    a[2] = __fadd_rn(a[2], b2);
-                    a[3] = __fadd_rn(a[3], b3);
-                }
+            auto write_dw = [&](int row, int c4, const float (&a)[4]) {
                 const int m = mrow0 + row;
-                if (m >= Mext) continue;
+                if (m >= Mext) return;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
                     const int col = ncol0 + 4 * c4 + q;
@@ -358,6 +349,75 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
                     const size_t o = p.layout == 0 ? ((size_t) ci * khw + tap) * p.kn + co
                                                    : ((size_t) co * p.C + ci) * khw + tap;
                     p.dw[o] = a[q];
+                }
+            };
+            for (int e = threadIdx.x; e < nr * (BN / 4); e += 128) {
+                const int rr = row_fast ? e % nr : e / (BN / 4), c4 = row_fast ? e / nr : e % (BN / 4);
+                const int row = r0 + rr;
+                const uint32_t off = (uint32_t) ((row * (BN + 4) + 4 * c4) * 4);
+                // every rank's four values in flight at once, then added in rank order
+                float4 b[16];
+#pragma unroll
+                for (int z = 0; z < 16; z++) {
+                    if (z < (int) nrank) {
+                        uint32_t ra;
+                        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(Rloc + off), "r"(z));
+                        asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(b[z].x), "=f"(b[z].y), "=f"(b[z].z), "=f"(b[z].w)
+                                     : "r"(ra));
+                    }
+                }
+                float a[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int z = 0; z < 16; z++) {
+                    if (z < (int) nrank) {
+                        a[0] = __fadd_rn(a[0], b[z].x);
+                        a[1] = __fadd_rn(a[1], b[z].y);
+                        a[2] = __fadd_rn(a[2], b[z].z);
+                        a[3] = __fadd_rn(a[3], b[z].w);
+                    }
+                }
+                if (G > 1)
+                    __stcg(reinterpret_cast<float4 *>(gslice + (size_t) row * BN + 4 * c4), make_float4(a[0], a[1], a[2], a[3]));
+                else
+                    write_dw(row, c4, a);
+            }
+            if (G > 1) {
+                // publish this slice, then count the tile's arrivals at this rank's slice
+                __threadfence();
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                __shared__ int s_last;
+                if (threadIdx.x == 0) {
+                    unsigned *cnt = p.counters + (size_t) tile * nrank + rank;
+                    const unsigned old = atomicAdd(cnt, 1u);
+                    s_last = old == (unsigned) (G - 1);
+                    if (s_last) atomicExch(cnt, 0u);   // every group has arrived: zero for the next call
+                    __threadfence();
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                if (s_last) {
+                    for (int e = threadIdx.x; e < nr * (BN / 4); e += 128) {
+                        const int rr = row_fast ? e % nr : e / (BN / 4), c4 = row_fast ? e / nr : e % (BN / 4);
+                        const int row = r0 + rr;
+                        const float *src = p.gws + ((size_t) tile * G * 128 + row) * BN + 4 * c4;
+                        float a[4] = {0.f, 0.f, 0.f, 0.f};
+                        for (int g0 = 0; g0 < G; g0 += 8) {
+                            float4 v[8];
+#pragma unroll
+                            for (int j = 0; j < 8; j++)
+                                if (g0 + j < G) v[j] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t) (g0 + j) * 128 * BN));
+#pragma unroll
+                            for (int j = 0; j < 8; j++) {
+                                if (g0 + j < G) {
+                                    a[0] = __fadd_rn(a[0], v[j].x);
+                                    a[1] = __fadd_rn(a[1], v[j].y);
+                                    a[2] = __fadd_rn(a[2], v[j].z);
+                                    a[3] = __fadd_rn(a[3], v[j].w);
+                                }
+                            }
+                        }
+                        write_dw(row, c4, a);
+                    }
                 }
             }
         }
@@ -480,7 +540,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = 1;
     at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = grid.z;
+    at[0].val.clusterDim.z = p.groups > 1 ? p.csize : grid.z;
     cfg.attrs = at;
     cfg.numAttrs = 1;
     cg_note_launch();
@@ -558,6 +618,35 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
 }
 
 }  // namespace
+
+namespace {
+// Tile counters of the grouped cluster reduction: zero at load, and every launch leaves the
+// words it used at zero (the last cluster of each tile resets its counter).  Launches take
+// consecutive ranges in turn, so that work queued on different streams uses different words.
+constexpr int WG_COUNTERS = 1 << 16;
+__device__ unsigned g_wgrad_counters[WG_COUNTERS];
+std::mutex g_cnt_mu;
+unsigned *g_cnt_base[64];
+int g_cnt_next[64];
+}  // namespace
+
+unsigned *tc_wgrad_counters(int n) {
+    int dev = 0;
+    if (n <= 0 || n > WG_COUNTERS || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_cnt_mu);
+    if (!g_cnt_base[dev]) {
+        void *a = nullptr;
+        if (cudaGetSymbolAddress(&a, g_wgrad_counters) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_cnt_base[dev] = (unsigned *) a;
+    }
+    if (g_cnt_next[dev] + n > WG_COUNTERS) g_cnt_next[dev] = 0;
+    unsigned *r = g_cnt_base[dev] + g_cnt_next[dev];
+    g_cnt_next[dev] += (n + 31) / 32 * 32;
+    return r;
+}
 
 bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits) {
     if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;

@@ -23,6 +23,14 @@ struct TcWgradParams {
     // 2..8 splits as one thread-block cluster along z: the partial tiles meet in
     // distributed shared memory and the cluster writes dW (no workspace, no reduction launch)
     int cluster;
+    // more splits than one cluster holds: `groups` clusters of `csize` splits per tile
+    // (cluster dimension z = csize, splits = groups * csize).  Rank r of each cluster writes
+    // its row slice of the cluster's sum to gws [tile][group][128][BN]; the last cluster to
+    // arrive at counter [tile][r] adds the groups' slices in group order and writes dW, then
+    // puts the counter back to zero.  groups = 0 or 1: one cluster per tile.
+    int groups, csize;
+    float *gws;
+    unsigned *counters;       // mtiles * ntiles * csize words, zero between calls
 };
 
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
@@ -30,6 +38,9 @@ cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, co
                             int mtiles, int ntiles, int splits, cudaStream_t st);
 // Whether splits (2..8) can run as clusters for this tile width / operand side.
 bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits);
+// Tile counters of the grouped cluster reduction on the current device: `n` consecutive
+// zero words for one launch (a rotating range of a fixed device array; NULL if unavailable).
+unsigned *tc_wgrad_counters(int n);
 // Split groups of the two-pass reduction (0: one pass).  With many splits, the
 // first pass sums each of G contiguous split ranges into planes that follow the
 // split planes in the workspace, so the workspace holds splits + G planes.

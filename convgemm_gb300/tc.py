@@ -113,6 +113,11 @@ WGRAD_X_ON_A = 0x10000      # weight-gradient aux flags: X as the A operand of a
 WGRAD_IM2COL_X = 0x20000    # X of a 1x1 stride-1 unpadded layer by im2col instead of tiled boxes
 
 
+def WGRAD_GROUPS(csize: int) -> int:
+    """Weight-gradient aux flag: more than 8 splits reduced inside the kernel by clusters of csize (2/4/8)."""
+    return {2: 0x100000, 4: 0x200000, 8: 0x300000}[csize]
+
+
 def tune_set(op: int, shape: Shape, bn: int = 0, splits: int = 0):
     """Overrides the tile heuristics for one operation on one shape (0, 0 removes the entry)."""
     _raise_if(lib().convgemm_tune_set(op, ctypes.byref(shape), bn, splits))
@@ -174,6 +179,28 @@ class GroupConv(ctypes.Structure):
     """convgemm_group_conv_t (include/convgemm_gpu.h)."""
     _fields_ = [("shape", Shape), ("x", ctypes.c_void_p), ("w", ctypes.c_void_p), ("y", ctypes.c_void_p),
                 ("scale", ctypes.c_void_p), ("shift", ctypes.c_void_p), ("relu", ctypes.c_int), ("bn", ctypes.c_int)]
+
+
+CACHE_BF16_FWD, CACHE_BF16_DGRAD, CACHE_FP8_FWD = 0, 1, 2
+
+
+def weights_cached(layout, shape: Shape, kind: int, weights, version: int, stream=None):
+    """Device address of the cached packed operand of FP32 `weights` (re-packed only when
+    `version` changed since it was packed); for CACHE_FP8_FWD, (packed, wscale) addresses."""
+    packed, wscale = ctypes.c_void_p(), ctypes.c_void_p()
+    _raise_if(lib().convgemm_weights_cached(layout, ctypes.byref(shape), kind, ptr(weights),
+                                            ctypes.c_ulonglong(version), ctypes.byref(packed),
+                                            ctypes.byref(wscale), _stream(stream)))
+    return (packed.value, wscale.value) if kind == CACHE_FP8_FWD else packed.value
+
+
+def weights_cache_evict(weights=None) -> int:
+    """Frees the cached operands of `weights` (all entries when None); returns how many."""
+    return lib().convgemm_weights_cache_evict(ptr(weights) if weights is not None else None)
+
+
+def weights_cache_bytes() -> int:
+    return lib().convgemm_weights_cache_bytes()
 
 
 def group_weights_size(shape: Shape) -> int:

@@ -10,6 +10,7 @@ convgemm_dgrad_bf16) and dW (FP32, through convgemm_wgrad_bf16, deterministic)
 of the convolution itself (ReLU and the scale apply to dY first).  There is no
 fallback: the operator runs the library's kernels or raises.
 """
+import weakref
 from typing import Optional, Tuple
 
 import torch
@@ -18,6 +19,41 @@ from . import NHWC, Shape
 from . import tc
 
 _LIB = "convgemm"
+
+# Packed-weight caching for repeated calls on unchanged weights (off by default).  When on,
+# a contiguous FP32 weight tensor's packed operands come from the library's cache, keyed
+# on its address and re-packed when its _version changes (an optimizer step, any in-place
+# write); the entries are evicted when the tensor is freed, before its address can be reused.
+_CACHE = {"on": False, "tracked": {}}
+
+
+def cache_weights(on: bool = True) -> bool:
+    """Turns packed-weight caching of the operator on or off; returns the previous setting."""
+    prev = _CACHE["on"]
+    _CACHE["on"] = bool(on)
+    if not on:
+        for addr in list(_CACHE["tracked"]):
+            tc.weights_cache_evict(addr)
+        _CACHE["tracked"].clear()
+    return prev
+
+
+def _evict(addr):
+    if _CACHE["tracked"].pop(addr, None) is not None:
+        tc.weights_cache_evict(addr)
+
+
+def _packed(s, kind, w):
+    """(packed operand address or tensor, keep-alive) for the FP32 weights w."""
+    if _CACHE["on"] and w.is_contiguous() and w.dtype == torch.float32:
+        addr = w.data_ptr()
+        if addr not in _CACHE["tracked"]:
+            _CACHE["tracked"][addr] = weakref.finalize(w, _evict, addr)
+        return tc.weights_cached(NHWC, s, kind, w, w._version)
+    op = tc.OPERAND_FWD if kind == tc.CACHE_BF16_FWD else tc.OPERAND_DGRAD
+    wp = torch.empty(max(1, tc.weights_size(s, op) // 2), dtype=torch.bfloat16, device=w.device)
+    tc.pack_weights(NHWC, s, op, w.contiguous(), wp)
+    return wp
 
 
 def _shape(x, w, stride, pad, dil):
@@ -32,8 +68,7 @@ def _shape(x, w, stride, pad, dil):
 def conv2d_nhwc(x: torch.Tensor, w: torch.Tensor, scale: Optional[torch.Tensor], shift: Optional[torch.Tensor],
                 stride: int, pad: int, dil: int, relu: bool) -> torch.Tensor:
     s = _shape(x, w, stride, pad, dil)
-    wp = torch.empty(tc.weights_size(s, tc.OPERAND_FWD) // 2, dtype=torch.bfloat16, device=x.device)
-    tc.pack_weights(NHWC, s, tc.OPERAND_FWD, w.contiguous(), wp)
+    wp = _packed(s, tc.CACHE_BF16_FWD, w)
     y = torch.empty(s.b, s.ho, s.wo, s.kn, dtype=torch.bfloat16, device=x.device)
     tc.fwd_bf16(s, x.contiguous(), wp, y, scale, shift, relu=relu)
     return y
@@ -55,8 +90,7 @@ def conv2d_nhwc_backward(dy: torch.Tensor, x: torch.Tensor, w: torch.Tensor, str
     s = _shape(x, w, stride, pad, dil)
     dy = dy.contiguous()
     dx = torch.empty_like(x)
-    wpd = torch.empty(max(1, tc.weights_size(s, tc.OPERAND_DGRAD) // 2), dtype=torch.bfloat16, device=x.device)
-    tc.pack_weights(NHWC, s, tc.OPERAND_DGRAD, w.contiguous(), wpd)
+    wpd = _packed(s, tc.CACHE_BF16_DGRAD, w)
     tc.dgrad_bf16(s, dy, wpd, dx)
     ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device=x.device)
     dw = torch.empty_like(w, dtype=torch.float32)

@@ -182,6 +182,31 @@ convgemm_status_t convgemm_fwd_bf16x3(const convgemm_shape_t *shape, const void 
                                       const void *w_hi, const void *w_lo, float *y, const float *scale,
                                       const float *shift, int relu, void *stream);
 
+/* ------------------------------------------------------ packed-weight cache */
+
+/* Operand kinds the cache keeps. */
+#define CONVGEMM_CACHE_BF16_FWD 0    /* convgemm_bf16_pack_weights(..., CONVGEMM_OPERAND_FWD, ...) */
+#define CONVGEMM_CACHE_BF16_DGRAD 1  /* convgemm_bf16_pack_weights(..., CONVGEMM_OPERAND_DGRAD, ...) */
+#define CONVGEMM_CACHE_FP8_FWD 2     /* convgemm_fp8_pack_weights: packed E4M3 + kn per-channel scales */
+
+/* The packed tensor-core operand of FP32 `weights` (reference layout of `layout`),
+ * from a library-owned cache keyed on (device, weights pointer, layout, shape, kind).
+ * The reference packs its weight operand on every call (pack_RB, src/gemm_blis.c:40-88);
+ * here an entry is packed once and re-packed on `stream` only when `version` differs
+ * from the one it was packed at (a caller-kept counter bumped whenever the weights
+ * change, e.g. a torch tensor's _version).  A hit launches nothing.  *packed (and for
+ * CONVGEMM_CACHE_FP8_FWD *wscale) stay valid until the entry is evicted.  A miss
+ * allocates with cudaMalloc and is refused (CONVGEMM_ERROR_NOT_SUPPORTED) while
+ * `stream` is being captured: fill the cache before capturing. */
+convgemm_status_t convgemm_weights_cached(convgemm_layout_t layout, const convgemm_shape_t *shape, int kind,
+                                          const float *weights, unsigned long long version, const void **packed,
+                                          const float **wscale, void *stream);
+/* Frees every entry packed from `weights` (all entries when NULL); returns how many.
+ * It waits for device work still reading them (cudaFree). */
+int convgemm_weights_cache_evict(const float *weights);
+/* Device bytes the cache holds. */
+size_t convgemm_weights_cache_bytes(void);
+
 /* ------------------------------------------------ grouped weight preparation */
 
 /* One layer's preparation for the BF16 forms: pack its FP32 weights (reference
@@ -237,6 +262,13 @@ convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int b
  * the BF16 bound (the tiled / im2col choice gives the same bits). */
 #define CONVGEMM_WGRAD_X_ON_A 0x10000
 #define CONVGEMM_WGRAD_IM2COL_X 0x20000
+/* Weight gradient with more than 8 splits: instead of the separate fixed-order reduction
+ * kernels, reduce inside the kernel with clusters of 2, 4 or 8 splits (their partial tiles
+ * summed through distributed shared memory, the clusters' sums added by the last cluster of
+ * each tile to arrive): CONVGEMM_WGRAD_GROUPS(2 / 4 / 8).  The split count is rounded up to
+ * a multiple of the cluster size.  The sum order is fixed by the split count and cluster
+ * size, so dW stays bit-reproducible. */
+#define CONVGEMM_WGRAD_GROUPS(csize) ((csize) == 8 ? 0x300000 : (csize) == 4 ? 0x200000 : (csize) == 2 ? 0x100000 : 0)
 void convgemm_tune_clear(void);
 
 /* ----------------------------------------- grouped persistent forward launch */

@@ -305,6 +305,64 @@ def test_wgrad_operand_forms(cglib, oracle_lib, b, h, w, c, kn, k, st, pad):
         tc.tune_clear()
 
 
+@pytest.mark.parametrize("b,h,w,c,kn,k,st,pad,splits", [
+    (8, 56, 56, 64, 64, 1, 1, 0, 143),    # 64-wide tiles, X is A: 18 clusters of 8, last one partly empty
+    (8, 28, 28, 128, 128, 3, 1, 1, 16),   # two clusters of 8 per tile
+    (4, 28, 28, 512, 256, 1, 1, 0, 19),   # 19 splits -> 3 clusters of 8 (5 empty splits)
+    (8, 28, 28, 256, 96, 3, 2, 1, 12),    # strided, kn = 96, ragged N tile
+])
+def test_wgrad_grouped_cluster_reduction(cglib, oracle_lib, b, h, w, c, kn, k, st, pad, splits):
+    """More than 8 pixel splits, reduced by the separate fixed-order kernels (the default) or inside
+    the kernel: clusters of 2 / 4 / 8 splits summed in distributed shared memory, the clusters'
+    sums added by the last cluster of each tile to arrive (no reduction launch).  Each within FP32
+    accumulation of FP64 on the same BF16 inputs, in both dW layouts, and bit-reproducible."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, st, st)
+    g = C.geom(b, h, w, c, kn, k, k, stride=st, pad=pad)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(83 + splits)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * ho * wo * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, ho, wo)
+    ref = O.wgrad_f64(C.NHWC, g, bf16r(dy), bf16r(x))
+    ref_nchw = O.wgrad_f64(C.NCHW, g, np.ascontiguousarray(bf16r(dy).reshape(b, ho, wo, kn).transpose(0, 3, 1, 2)).ravel(),
+                           np.ascontiguousarray(bf16r(x).reshape(b, h, w, c).transpose(0, 3, 1, 2)).ravel())
+    K = c * k * k
+    n0 = cg.lib().convgemm_launch_count()
+
+    def run(aux, layout):
+        tc.tune_set(tc.TUNE_WGRAD, s, 0, aux)
+        ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+        d = torch.full((K * kn,), float("nan"), device="cuda")
+        c0 = cg.lib().convgemm_launch_count()
+        tc.wgrad_bf16(layout, s, dyd, xd, d, ws)
+        launches = cg.lib().convgemm_launch_count() - c0
+        torch.cuda.synchronize()
+        cg.check_device()
+        return d, launches
+
+    try:
+        kern, nk = run(splits, cg.NHWC)   # default: the separate reduction kernels
+        assert tc.wgrad_bf16_plan(s)[1] > 8
+        assert nk >= 2
+        assert rel_max_rms(kern.cpu().numpy(), ref)[0] <= 1e-4
+        for cs in (2, 4, 8):
+            grouped, nl = run(splits | tc.WGRAD_GROUPS(cs), cg.NHWC)
+            plan = tc.wgrad_bf16_plan(s)
+            assert plan[1] % cs == 0 and plan[1] >= splits // 2, (cs, plan)
+            assert nl == 1, "the grouped reduction needs no reduction launch"
+            again, _ = run(splits | tc.WGRAD_GROUPS(cs), cg.NHWC)
+            assert torch.equal(grouped, again), "bit-reproducible"
+            assert rel_max_rms(grouped.cpu().numpy(), ref)[0] <= 1e-4, cs
+            nchw, _ = run(splits | tc.WGRAD_GROUPS(cs), cg.NCHW)
+            assert rel_max_rms(nchw.cpu().numpy(), ref_nchw)[0] <= 1e-4, cs
+    finally:
+        tc.tune_clear()
+    assert cg.lib().convgemm_launch_count() > n0
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc

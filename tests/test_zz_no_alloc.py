@@ -16,6 +16,7 @@ kernel, is checked against the FP64 oracle as well.  This file is collected last
 on purpose.
 """
 import ctypes
+import gc
 
 import numpy as np
 import pytest
@@ -122,6 +123,8 @@ def test_noalloc_allocates_nothing(cglib):
     x, dy = _inputs(tc, s, 3)
     out = torch.empty(s.c * 9 * s.kn, device="cuda")
     _noalloc(cg, cg.NHWC, s, dy, x, out)   # the first call of this shape loads its kernels
+    torch.cuda.synchronize()
+    gc.collect()   # tensors of earlier tests freed now, not during the measured call
     torch.cuda.synchronize()
     a0, (f0, _) = torch.cuda.memory_allocated(), torch.cuda.mem_get_info()
     _noalloc(cg, cg.NHWC, s, dy, x, out)
