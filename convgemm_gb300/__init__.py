@@ -154,6 +154,11 @@ def lib():
         L.convgemm_weights_cache_evict.argtypes = [_VP]
         L.convgemm_weights_cache_evict.restype = _I
         L.convgemm_weights_cache_bytes.restype = ctypes.c_size_t
+        L.convgemm_measure_ffma.argtypes = [_I, _VP, ctypes.POINTER(ctypes.c_double), _VP]
+        L.convgemm_tune_describe.argtypes = [_I, SP] + [ctypes.POINTER(_I)] * 4
+        L.convgemm_dgrad_bf16_bias_grad_workspace_size.argtypes = [SP]
+        L.convgemm_dgrad_bf16_bias_grad_workspace_size.restype = ctypes.c_size_t
+        L.convgemm_dgrad_bf16_bias_grad.argtypes = [SP, _VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_size_t, _VP]
         _lib = L
     return _lib
 

@@ -29,8 +29,8 @@ from . import tc
 
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
-OP_CACHE_TAG = "v5"   # op entries: fwd / dgrad with the M-tile and epilogue-warp choices
-WGRAD_CACHE_TAG = "v6"   # wgrad: 2-chunk stages, direct single-split writes, 2..8-split clusters, grouped clusters
+OP_CACHE_TAG = "v6"   # op entries: fwd / dgrad with the M-tile, epilogue-warp and ring-stage choices
+WGRAD_CACHE_TAG = "v8"   # wgrad: ring stages, direct single-split writes, 2..8-split clusters, grouped clusters, slab kernel
 
 
 def cache_path() -> str:
@@ -175,13 +175,17 @@ def graph_time_us(run, reps: int = 10) -> float:
 
 def _mt_ew(widths):
     """(bn, aux) of the BF16 forward / input gradient: aux = M tiles sharing a weight tile (1 / 2),
-    + 4 for eight epilogue warps (bn >= 128 or two M tiles, not bn 256 with two)."""
+    + 4 for eight epilogue warps (bn >= 128 or two M tiles, not bn 256 with two), and for one M
+    tile with four epilogue warps at widths 64 / 128 also the ring of one K block per stage with
+    twice the stages (+ CONV_STAGES1)."""
     out = []
     for w in widths:
         for m in (1, 2):
             out.append((w, m))
             if (w >= 128 or m == 2) and not (w == 256 and m == 2):
                 out.append((w, m + 4))
+        if w != 256:
+            out.append((w, 1 | tc.CONV_STAGES1))
     return out
 
 
@@ -211,8 +215,18 @@ def op_candidates(op: int, s):
                 for sp in sorted({max(1, s2 // 2), s2, min(mx, 2 * s2)} | {x for x in (2, 4, 8) if x <= mx}):
                     out.append((w, sp | tc.WGRAD_X_ON_A))
             tc.tune_set(op, s, 0, 0)
+    # the ring of one chunk per stage with twice the stages (im2col path), for every tile and split
+    if tc.c8(s.c) % 64 == 0:
+        out += [(w, sp | tc.WGRAD_STAGES1) for w, sp in list(out)]
     # more than 8 splits: also the in-kernel reduction by clusters of 2 / 4 / 8 splits
-    out += [(w, sp | tc.WGRAD_GROUPS(cs)) for w, sp in list(out) if (sp & 0xffff) > 8 for cs in (2, 4, 8)]
+    out += [(w, sp | tc.WGRAD_GROUPS(cs)) for w, sp in list(out)
+            if (sp & 0xffff) > 8 and not sp & tc.WGRAD_STAGES1 for cs in (2, 4, 8)]
+    # stride-1 layers with 128-channel blocks: the slab kernel around its own split heuristic
+    tc.tune_set(op, s, 0, tc.WGRAD_SLAB)
+    bn_s, s3, _ = tc.wgrad_bf16_plan(s)
+    tc.tune_set(op, s, 0, 0)
+    if s.vstride == 1 and s.hstride == 1 and tc.c8(s.c) % 128 == 0 and s.kw >= 2 and s.kn >= 64:
+        out += [(0, tc.WGRAD_SLAB | sp) for sp in sorted({max(1, s3 // 2), s3, min(mx, 2 * s3)})]
     return out
 
 
@@ -258,7 +272,11 @@ def tune_ops(items, path: str | None = None, force: bool = False, measure_missin
             if best is None:
                 stats["heuristic"] += 1
                 continue
-            entry, src = {"bn": best[1], "splits": best[2], "us": times}, "measured"
+            tc.tune_set(op, s, best[1], best[2])
+            kern, bnd, stages, cluster = tc.tune_describe(op, s) if op in (tc.TUNE_FWD, tc.TUNE_DGRAD, tc.TUNE_WGRAD) \
+                else (0, best[1], 0, 1)
+            entry, src = {"bn": best[1], "splits": best[2], "kernel": kern, "stages": stages, "cluster": cluster,
+                          "us": times}, "measured"
             table[k] = entry
             dirty = True
         else:

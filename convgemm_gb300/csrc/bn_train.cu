@@ -55,6 +55,16 @@ __global__ void bn_stats_pass2(const double *__restrict__ chunks, int nchunks, i
     stats[i] = a;
 }
 
+// Column sums in FP32 from the chunk sums of pass 1: out[c] = sum over the chunks, in order,
+// of the first statistics plane.
+__global__ void colsum_pass2_f32(const double *__restrict__ chunks, int nchunks, int kn, float *__restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= kn) return;
+    double a = 0.0;
+    for (int j = 0; j < nchunks; j++) a += chunks[(size_t) j * 2 * kn + c];
+    out[c] = (float) a;
+}
+
 __global__ void bn_fold_kernel(int kn, const double *__restrict__ stats, double inv_count, const float *gamma,
                                const float *beta, float eps, float *scale, float *shift, float *mean_out,
                                float *var_out) {
@@ -113,6 +123,23 @@ size_t stats_ws_bytes(const cg_shape &s) {
 }
 
 }  // namespace
+
+size_t cg_colsum_ws_bytes(long long ngroups, int kn) {
+    const long long nchunks = (ngroups + BN_CHUNK - 1) / BN_CHUNK;
+    return (size_t) (nchunks * 2 * kn * 8 + ngroups * 2 * kn * 4);
+}
+
+cudaError_t cg_colsum_reduce(void *workspace, int ngroups, int kn, float *out, cudaStream_t st) {
+    const int nchunks = (ngroups + BN_CHUNK - 1) / BN_CHUNK;
+    double *chunks = (double *) workspace;
+    const float *part = (const float *) ((uint8_t *) workspace + (size_t) nchunks * 2 * kn * 8);
+    dim3 g1((kn + 31) / 32, nchunks);
+    bn_stats_pass1<<<g1, 256, 0, st>>>(part, ngroups, kn, chunks);
+    cg_note_launch();
+    colsum_pass2_f32<<<(kn + 127) / 128, 128, 0, st>>>(chunks, nchunks, kn, out);
+    cg_note_launch();
+    return cudaGetLastError();
+}
 
 extern "C" size_t convgemm_fwd_bf16_stats_workspace_size(const convgemm_shape_t *shape) {
     if (!shape || shape->b < 1 || shape->kn < 1 || shape->c < 1) return 0;

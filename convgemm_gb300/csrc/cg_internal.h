@@ -33,6 +33,15 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
 cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const float *dy, float *dx,
                           int accumulate, cudaStream_t st);
 
+// Fixed-order column sums of per-32-row-group statistics partials (bn_train.cu): the workspace
+// holds the FP64 chunk sums, then the FP32 partials [ngroups][2][kn] the kernel writes (at
+// workspace + the chunk bytes); out[c] = the sum of plane 0 over the groups, in FP32.
+size_t cg_colsum_ws_bytes(long long ngroups, int kn);
+cudaError_t cg_colsum_reduce(void *workspace, int ngroups, int kn, float *out, cudaStream_t st);
+inline size_t cg_colsum_part_offset(long long ngroups, int kn) {
+    return (size_t) ((ngroups + 255) / 256) * 2 * kn * 8;   // 256 groups per chunk (bn_train.cu)
+}
+
 // Device error word (set by bounded waits); defined in cg_runtime.cu.
 int *cg_device_error_word();
 // Counts one kernel launch made by the library (convgemm_launch_count).

@@ -128,7 +128,7 @@ struct Tile {
 // kernel parameters with a runtime class index would cost generic-memory loads
 // on every tile).
 struct ClsS {
-    int Hg, Wg, oy0, ox0, osy, osx, isy, isx, iby, ibx, ntaps, kbeg, ktiles, tile0, lo_y, lo_x, mint_y, mint_x;
+    int Hg, Wg, oy0, ox0, osy, osx, isy, isx, iby, ibx, ntaps, kbeg, ktiles, tile0, lo_y, lo_x, mint_y, mint_x, gbase;
     FastDiv dwg, dhg;
 };
 static_assert(sizeof(ClsS) <= 128, "class table entry");
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
         d.Hg = c.Hg; d.Wg = c.Wg; d.oy0 = c.oy0; d.ox0 = c.ox0; d.osy = c.osy; d.osx = c.osx;
         d.isy = c.isy; d.isx = c.isx; d.iby = c.iby; d.ibx = c.ibx; d.ntaps = c.ntaps; d.kbeg = c.kbeg;
         d.ktiles = c.ktiles; d.tile0 = c.tile0; d.lo_y = c.lo_y; d.lo_x = c.lo_x; d.mint_y = c.mint_y;
-        d.mint_x = c.mint_x; d.dwg = c.dwg; d.dhg = c.dhg;
+        d.mint_x = c.mint_x; d.gbase = c.gbase; d.dwg = c.dwg; d.dhg = c.dhg;
     }
     // everything above touched only shared memory and kernel parameters; the next kernel may
     // launch once every CTA has started its last tile (pdl_trigger in the producer loop), so
@@ -405,9 +405,35 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                 }
                 const int nb = tl.n0 + c0;
                 if constexpr (STATS) if (m0 + ew * 32 < M) {
-                    // batch-norm statistics of this chunk's 64 columns over the warp's 32 rows
-                    // (group (m0 + 32 ew) / 32 of the ceil(M / 32) the workspace holds)
-                    float *part = p.stats + (size_t) ((m0 >> 5) + ew) * 2 * p.Cout;
+                    // column statistics of this chunk's 64 columns over the warp's 32 rows (group
+                    // gbase + (m0 + 32 ew) / 32 of the class; the classes' groups are concatenated):
+                    // the forward's batch-norm sums, or, for the masked input gradient, the sums of
+                    // the masked output (the bias gradient of the layer that produced the mask)
+                    if (p.mask && m < M && nb < p.Cout) {
+                        size_t pix = (size_t) m;
+                        if (!p.epi_tma) {
+                            uint32_t q, jw, j, b;
+                            cl.dwg.divmod(m, q, jw);
+                            cl.dhg.divmod(q, b, j);
+                            pix = ((size_t) b * p.Hout + cl.oy0 + cl.osy * (int) j) * p.Wout + cl.ox0 + cl.osx * (int) jw;
+                        }
+                        const __nv_bfloat16 *mrow = p.mask + pix * p.Cout + nb;
+#pragma unroll
+                        for (int q = 0; q < 8; q++) {
+                            uint4 mv = make_uint4(0, 0, 0, 0);
+                            if (nb + 8 * q + 8 <= p.Cout) mv = __ldg(reinterpret_cast<const uint4 *>(mrow) + q);
+                            const uint32_t mw[4] = {mv.x, mv.y, mv.z, mv.w};
+#pragma unroll
+                            for (int e = 0; e < 4; e++) {
+                                const int jj = 8 * q + 2 * e;
+                                uint32_t &lo = jj < 32 ? v0[jj] : v1[jj - 32];
+                                uint32_t &hi = jj + 1 < 32 ? v0[jj + 1] : v1[jj - 31];
+                                if ((mw[e] & 0xFFFFu) - 1u >= 0x7F80u) lo = 0u;   // mask <= 0 (or NaN)
+                                if ((mw[e] >> 16) - 1u >= 0x7F80u) hi = 0u;
+                            }
+                        }
+                    }
+                    float *part = p.stats + (size_t) (cl.gbase + (m0 >> 5) + ew) * 2 * p.Cout;
 #pragma unroll
                     for (int h = 0; h < 2; h++) {
                         float sum, sq;
@@ -624,6 +650,14 @@ cudaError_t launch_bn(const TcConvParams &p, const CUtensorMap &wmap, const CUte
 // BN=128 3 x 2, BN=256 3 x 1 with two output staging buffers (its tiles are often
 // single-block 1x1 layers bound by the output stores).  FP8 blocks are half the bytes,
 // 3xBF16 blocks twice.
+int tc_conv_stages(int bn, int im2col, int mt, int ew, int kb1) {
+    if (!im2col) return bn == 64 ? 8 : (bn == 128 ? 6 : 4);
+    if (ew == 8) return mt == 2 ? 3 : (bn == 128 ? 4 : 3);
+    if (mt == 2) return bn == 256 ? 3 : 4;
+    if (kb1 && bn != 256) return bn == 64 ? 8 : 6;
+    return bn == 64 ? 4 : 3;
+}
+
 cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
                            const TcMaps &amaps, int grid, cudaStream_t st) {
     if (p.mode == MODE_FP8) {
@@ -685,6 +719,13 @@ cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const
         }
     }
     if (p.mt != 1) return cudaErrorInvalidValue;
+    if (p.im2col && p.kb1) {
+        switch (p.bn) {
+            case 64: return launch_bn<64, 8, 1, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 6, 1, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);
+            default: break;   // 256-wide tiles keep their three one-block stages
+        }
+    }
     if (p.im2col) {
         switch (p.bn) {
             case 64: return launch_bn<64, 4, 2, true, MODE_BF16>(p, wmap, omap, amaps, grid, st);

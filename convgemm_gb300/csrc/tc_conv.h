@@ -21,6 +21,7 @@ struct TcClass {
     int ktiles;  // K / 64
     int mtiles;  // ceil(B*Hg*Wg / 128)
     int tile0;   // index of the class's first tile in the launch (classes' tiles are concatenated)
+    int gbase;   // statistics form: the class's first 32-row group (classes' groups are concatenated)
     // im2col-mode TMA: first pixel of row j sits at (j*isy + lo_y, jw*isx + lo_x) in the gathered
     // tensor and tap t is the unsigned offset (toy[t] - mint_y, tox[t] - mint_x)
     int lo_y, lo_x, mint_y, mint_x;
@@ -51,6 +52,8 @@ struct TcConvParams {
     int mode;                  // 0 BF16, 1 FP8-E4M3, 2 3xBF16 (FP32 output)
     int mt;                    // 128-row M tiles per tile (1, or 2 sharing each weight tile: BF16 im2col only)
     int ew;                    // epilogue warps: 4, or 8 (BF16 im2col, bn >= 128 or mt == 2, not bn 256 with mt 2)
+    int kb1;                   // BF16 im2col, one M tile, four epilogue warps, bn 64 / 128: one K block per ring
+                               // stage and twice the stages (8 / 6) instead of two blocks per stage (4 / 3)
     int ncls;
     TcClass cls[TC_MAXCLS];
 };
@@ -64,5 +67,7 @@ struct TcMaps {
 };
 
 // wmap: packed weights [Cout][K] (box 64 x bn); omap: output [pixels][Cout] (box 64 x 128), used when epi_tma.
+// Ring stages of the BF16 implicit-GEMM kernel form chosen by these settings.
+int tc_conv_stages(int bn, int im2col, int mt, int ew, int kb1);
 cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const CUtensorMap &omap,
                            const TcMaps &amaps, int grid, cudaStream_t st);

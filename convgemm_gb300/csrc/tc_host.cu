@@ -394,11 +394,16 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
         p.mt = 1;
         p.ew = 4;
     }
-    int t0 = 0;
+    // aux bit 4 (tuning): one K block per ring stage, twice the stages (BF16 im2col, one M tile,
+    // four epilogue warps, 64 / 128-wide tiles)
+    p.kb1 = (aux_override & 16) && mode == 0 && p.im2col && p.mt == 1 && p.ew == 4 && !stats && p.bn != 256;
+    int t0 = 0, g0 = 0;
     for (int c = 0; c < pl.ncls; c++) {
         p.cls[c] = pi.cls[c];
         p.cls[c].tile0 = t0;
+        p.cls[c].gbase = g0;   // statistics groups of 32 rows, classes concatenated
         t0 += (pl.cls[c].mtiles + p.mt - 1) / p.mt * p.ntiles;
+        g0 += (int) (((long long) s.b * pl.cls[c].Hg * pl.cls[c].Wg + 31) / 32);
     }
     p.ntiles_total = t0;
     const int grid = t0 < sms ? t0 : sms;
@@ -568,6 +573,53 @@ extern "C" convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *sh
     return dgrad_bf16(shape, dy, wpacked, dx, x, 0, stream);
 }
 
+namespace {
+long long dgrad_stat_groups(const TcPlan &pl, int b) {
+    long long g = 0;
+    for (int c = 0; c < pl.ncls; c++) g += ((long long) b * pl.cls[c].Hg * pl.cls[c].Wg + 31) / 32;
+    return g;
+}
+}  // namespace
+
+extern "C" size_t convgemm_dgrad_bf16_bias_grad_workspace_size(const convgemm_shape_t *shape) {
+    if (tc_check_shape(shape, "convgemm_dgrad_bf16_bias_grad_workspace_size") || shape->c % 8) return 0;
+    TcPlan pl;
+    if (!tc_plan_dgrad(cg_from_public(*shape), pl)) return 0;
+    return cg_colsum_ws_bytes(dgrad_stat_groups(pl, shape->b), shape->c);
+}
+
+extern "C" convgemm_status_t convgemm_dgrad_bf16_bias_grad(const convgemm_shape_t *shape, const void *dy,
+                                                           const void *wpacked, void *dx, const void *relu_x,
+                                                           float *db, void *workspace, size_t workspace_bytes,
+                                                           void *stream) {
+    const char *fn = "convgemm_dgrad_bf16_bias_grad";
+    if (convgemm_status_t e = tc_check_shape(shape, fn)) return e;
+    if (!dy || !wpacked || !dx || !db || !workspace)
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL argument", fn);
+    if (shape->c % 8) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: c must be a multiple of 8", fn);
+    if (relu_x && ((uintptr_t) relu_x & 15))
+        return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: relu_x not 16-byte aligned", fn);
+    const cg_shape s = cg_from_public(*shape);
+    TcPlan pl;
+    if (!tc_plan_dgrad(s, pl)) return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: more than 16 stride-phase classes", fn);
+    const long long ng = dgrad_stat_groups(pl, s.b);
+    const size_t need = cg_colsum_ws_bytes(ng, s.c);
+    if (workspace_bytes < need || ((uintptr_t) workspace & 15))
+        return cg_set_error(CONVGEMM_ERROR_WORKSPACE, "%s: workspace needs %zu bytes, 16-byte aligned", fn, need);
+    cudaStream_t st = (cudaStream_t) stream;
+    if (pl.has_empty_class)   // pixels no tap reaches: zero (and nothing to the sums)
+        if (convgemm_status_t e = cg_cuda_check(
+                cudaMemsetAsync(dx, 0, sizeof(__nv_bfloat16) * (size_t) s.b * s.h * s.w * s.c, st), "zero dx"))
+            return e;
+    TcTune t{0, 0};
+    tc_tune_get(CONVGEMM_TUNE_DGRAD, *shape, &t);
+    float *part = (float *) ((uint8_t *) workspace + cg_colsum_part_offset(ng, s.c));
+    if (convgemm_status_t e = tc_run(pl, s, dy, wpacked, dx, nullptr, nullptr, 0, st, 0, nullptr, nullptr, t.bn,
+                                     t.splits, relu_x, part, 0))
+        return e;
+    return cg_cuda_check(cg_colsum_reduce(workspace, (int) ng, s.c, db, st), "bias-gradient column sums");
+}
+
 extern "C" convgemm_status_t convgemm_dgrad_bf16_ex(const convgemm_shape_t *shape, const void *dy,
                                                     const void *wpacked, void *dx, const void *relu_x, int accumulate,
                                                     void *stream) {
@@ -584,6 +636,8 @@ namespace {
 struct WgPlan {
     int xa, bn, x2d, stem, mtiles, ntiles, splits, cps, nchunks, Nx, Cp, kn8;
     int csize, groups;   // grouped cluster reduction (groups > 1): splits = groups * csize
+    int slab;            // the slab kernel (tc_wgrad_slab.cu) with `splits` partials
+    int kb1;             // im2col path: one chunk per ring stage (twice the stages)
     size_t ws_bytes;
 };
 
@@ -606,6 +660,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.Nx = s.kh * s.kw * w.Cp;
     const bool im2col = wgrad_im2col_ok(s, g);
     const int aux_splits = t.splits & 0xffff;
+    w.kb1 = im2col && (t.splits & CONVGEMM_WGRAD_STAGES1) ? 1 : 0;
     // X on the A side: always for narrow layers, on request for wide ones (im2col path)
     const bool x_on_a = (t.splits & CONVGEMM_WGRAD_X_ON_A) && im2col;
     w.xa = s.kn < 128 || x_on_a;
@@ -641,7 +696,21 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         w.bn = 64;
         w.splits = tc_stem_wgrad_splits(s);
     }
+    // stride-1 layers with 128-channel input blocks: the slab kernel, by default (no tuning
+    // entry) or when the tuning entry asks for it
+    w.slab = 0;
+    if (!w.stem && ((t.bn == 0 && t.splits == 0) || (t.splits & CONVGEMM_WGRAD_SLAB))) {
+        const int sp = tc_wgrad_slab_splits(s, aux_splits, t.bn);
+        if (sp > 0) {
+            w.slab = 1;
+            w.splits = sp;
+            w.bn = tc_wgrad_slab_bn(s, t.bn);
+            w.xa = 1;
+        }
+    }
     w.ws_bytes = sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
+    w.csize = w.groups = 0;
+    if (w.slab) return w;
     // more splits than one cluster: clusters of up to 8 splits, reduced in the kernel (the
     // workspace is sized for the smallest cluster, so that it does not depend on the device)
     w.csize = w.groups = 0;
@@ -651,7 +720,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         if (grouped > w.ws_bytes) w.ws_bytes = grouped;
         const int code = (t.splits >> 20) & 3;   // CONVGEMM_WGRAD_GROUPS: 1, 2, 3 -> clusters of 2, 4, 8
         const int want = code ? 1 << code : 0;
-        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want) ? want : 0;
+        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want, w.kb1) ? want : 0;
         if (cs) {
             w.csize = cs;
             w.groups = (w.splits + cs - 1) / cs;
@@ -699,6 +768,12 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
                             workspace_bytes, w.ws_bytes);
     if (w.stem)
         return tc_stem_wgrad_run(s, dy, x, (float *) workspace, dw, layout == CONVGEMM_NCHW, (cudaStream_t) stream);
+    if (w.slab) {
+        TcTune t{0, 0};
+        tc_tune_get(CONVGEMM_TUNE_WGRAD, *shape, &t);
+        return tc_wgrad_slab_run(s, t.splits & 0xffff, t.bn, dy, x, (float *) workspace, dw,
+                                 layout == CONVGEMM_NCHW, (cudaStream_t) stream);
+    }
     CUtensorMap map;
     if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, w.kn8, 64, 64))
         return e;
@@ -749,6 +824,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.direct = w.splits == 1;
     p.layout = layout == CONVGEMM_NCHW;
     p.C = s.c;
+    p.kb1 = w.kb1;
     if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
         // clusters of csize splits; the tile's last cluster adds the clusters' sums
         p.cluster = 1;
@@ -758,7 +834,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         p.counters = tc_wgrad_counters(w.mtiles * w.ntiles * w.csize);
         if (!p.counters) return cg_set_error(CONVGEMM_ERROR_CUDA, "convgemm_wgrad_bf16: tile counters unavailable");
     } else {
-        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits);
+        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1);
     }
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
@@ -767,6 +843,71 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     return cg_cuda_check(tc_wgrad_reduce((float *) workspace, dw, w.splits, w.xa, w.Nx, s.kn, s.c, w.Cp, s.kh,
                                          s.kw, layout == CONVGEMM_NCHW, st),
                          "weight-gradient reduction");
+}
+
+// ---------------------------------------------------------- tuning report
+// What the tuning table (or the heuristic) selects for one operation on one shape: the kernel
+// (0 the general implicit GEMM, 1 a slab kernel, 2 the small-channel kernel), the tile width,
+// the ring stages of the general kernels (slab and small-channel kernels size their buffers at
+// run time: 0) and the cluster size (1, or the splits / cluster of a weight gradient).
+extern "C" convgemm_status_t convgemm_tune_describe(int op, const convgemm_shape_t *shape, int *kernel, int *bn,
+                                                    int *stages, int *cluster) {
+    const char *fn = "convgemm_tune_describe";
+    if (convgemm_status_t e = tc_check_shape(shape, fn)) return e;
+    if (!kernel || !bn || !stages || !cluster) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "%s: NULL output", fn);
+    const cg_shape s = cg_from_public(*shape);
+    TcTune t{0, 0};
+    *kernel = 0;
+    *bn = 0;
+    *stages = 0;
+    *cluster = 1;
+    if (op == CONVGEMM_TUNE_WGRAD) {
+        const WgPlan w = plan_wgrad(*shape);
+        *bn = w.bn;
+        if (w.stem || w.slab) {
+            *kernel = w.stem ? 2 : 1;
+            return CONVGEMM_SUCCESS;
+        }
+        const ConvGeom g = make_geom(s);
+        const int im2col = wgrad_im2col_ok(s, g);
+        *stages = tc_wgrad_stages(w.bn, im2col, w.kb1);
+        if (w.groups > 1) *cluster = w.csize;
+        else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1)) *cluster = w.splits;
+        return CONVGEMM_SUCCESS;
+    }
+    if (op != CONVGEMM_TUNE_FWD && op != CONVGEMM_TUNE_DGRAD)
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: forward, input gradient or weight gradient only", fn);
+    TcPlan pl;
+    if (op == CONVGEMM_TUNE_FWD) {
+        tc_plan_fwd(s, pl);
+        if (tc_stem_applicable(s)) {
+            *kernel = 2;
+            *bn = s.kn;
+            return CONVGEMM_SUCCESS;
+        }
+    } else if (!tc_plan_dgrad(s, pl)) {
+        return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED, "%s: more than 16 stride-phase classes", fn);
+    }
+    tc_tune_get(op, *shape, &t);
+    if (!(t.splits & 8) && tc_slab_applicable(pl)) {
+        *kernel = 1;
+        *bn = 64;
+        return CONVGEMM_SUCCESS;
+    }
+    TcPlan pi = pl;
+    const int im2col = tc_plan_im2col(pi);
+    *bn = t.bn ? t.bn : tc_pick_bn(pl, tc_num_sms());
+    const int mt = ((t.splits & 3) == 2 && im2col) ? 2 : 1;
+    bool ew8 = (t.splits & 4) != 0;
+    if ((t.splits & 7) == 0) {
+        int kmax = 0;
+        for (int c = 0; c < pl.ncls; c++) kmax = pl.cls[c].ktiles > kmax ? pl.cls[c].ktiles : kmax;
+        ew8 = kmax <= 8;
+    }
+    const int ew = (ew8 && im2col && (*bn >= 128 || mt == 2) && !(*bn == 256 && mt == 2)) ? 8 : 4;
+    const int kb1 = (t.splits & 16) && im2col && mt == 1 && ew == 4 && *bn != 256;
+    *stages = tc_conv_stages(*bn, im2col, mt, ew, kb1);
+    return CONVGEMM_SUCCESS;
 }
 
 // ------------------------------------------------- grouped weight preparation

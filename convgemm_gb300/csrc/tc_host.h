@@ -55,6 +55,14 @@ bool tc_stem_wgrad_applicable(const cg_shape &s);
 int tc_stem_wgrad_splits(const cg_shape &s);
 convgemm_status_t tc_stem_wgrad_run(const cg_shape &s, const void *dy, const void *x, float *ws, float *dw,
                                     int layout, cudaStream_t st);
+// Weight gradient of stride-1 convolutions with 128-channel input blocks from input slabs
+// (tc_wgrad_slab.cu): the number of FP32 partials for a requested split count (0: the
+// heuristic), 0 if the shape does not fit the kernel; and the run (partials into ws, then
+// the fixed-order reduction into dw; one split writes dw directly).
+int tc_wgrad_slab_splits(const cg_shape &s, int want_splits, int want_bn);
+int tc_wgrad_slab_bn(const cg_shape &s, int want_bn);   // output-channel tile width (64 / 128)
+convgemm_status_t tc_wgrad_slab_run(const cg_shape &s, int want_splits, int want_bn, const void *dy, const void *x,
+                                    float *ws, float *dw, int layout, cudaStream_t st);
 // Autotuned tile configuration of one operation on one shape (0 = heuristic):
 // bn = output channels per tile; splits = pixel splits of the weight gradient,
 // or M tiles per weight tile (1 or 2) of the forward / input gradient.

@@ -37,15 +37,15 @@ extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *s
     const bool mt_op = op == CONVGEMM_TUNE_FWD || op == CONVGEMM_TUNE_DGRAD;
     // forward / input gradient: M tiles per weight tile (1 / 2) + 4 for eight epilogue warps
     // weight gradient: pixel splits in bits 0-15, CONVGEMM_WGRAD_* flags above
-    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? (splits >= 0 && (splits & ~0x33ffff) == 0)
-                        : mt_op ? ((splits & ~8) == 0 || (splits & ~8) == 1 || (splits & ~8) == 2 ||
-                                   (splits & ~8) == 5 || (splits & ~8) == 6)
+    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? (splits >= 0 && (splits & ~0x7bffff) == 0)
+                        : mt_op ? ((splits & ~24) == 0 || (splits & ~24) == 1 || (splits & ~24) == 2 ||
+                                   (splits & ~24) == 5 || (splits & ~24) == 6)
                                 : splits == 0;
     if (!aux_ok)
         return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE,
                             "convgemm_tune_set: aux is the weight gradient's split count (plus CONVGEMM_WGRAD_* flags), or for the BF16 forward / "
                             "input gradient 1 / 2 M tiles per weight tile, plus 4 for eight epilogue warps, plus 8 for the general "
-                            "kernel instead of the slab kernel");
+                            "kernel instead of the slab kernel, plus 16 for one K block per ring stage");
     std::lock_guard<std::mutex> lk(g_tune_mu);
     if (bn == 0 && splits == 0)
         g_tune.erase(key_of(op, *shape));

@@ -586,6 +586,22 @@ template <bool IM2C>
 cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                           dim3 grid, cudaStream_t st) {
     if constexpr (IM2C) {
+        if (p.kb1) {   // one chunk per stage: 64-wide 4 stages of 24 KB, 128-wide 6 x 32 KB, 256-wide 4 x 48 KB
+            if (xa) {
+                switch (bn) {
+                    case 64: return launch_wg<64, 4, true, IM2C, 1>(p, dymap, xmap, grid, st);
+                    case 128: return launch_wg<128, 6, true, IM2C, 1>(p, dymap, xmap, grid, st);
+                    case 256: return launch_wg<256, 4, true, IM2C, 1>(p, dymap, xmap, grid, st);
+                    default: return cudaErrorInvalidValue;
+                }
+            }
+            switch (bn) {
+                case 64: return launch_wg<64, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
+                case 128: return launch_wg<128, 6, false, IM2C, 1>(p, dymap, xmap, grid, st);
+                case 256: return launch_wg<256, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
         if (xa) {
             switch (bn) {
                 case 64: return launch_wg<64, 2, true, IM2C, 2>(p, dymap, xmap, grid, st);
@@ -648,8 +664,16 @@ unsigned *tc_wgrad_counters(int n) {
     return r;
 }
 
-bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits) {
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1) {
     if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;
+    if (im2col && kb1) {
+        if (xa) return bn == 64    ? cluster_fits<64, 4, true, true, 1>(splits)
+                       : bn == 128 ? cluster_fits<128, 6, true, true, 1>(splits)
+                                   : bn == 256 && cluster_fits<256, 4, true, true, 1>(splits);
+        return bn == 64    ? cluster_fits<64, 4, false, true, 1>(splits)
+               : bn == 128 ? cluster_fits<128, 6, false, true, 1>(splits)
+                           : bn == 256 && cluster_fits<256, 4, false, true, 1>(splits);
+    }
     if (im2col) {
         if (xa) return bn == 64    ? cluster_fits<64, 2, true, true, 2>(splits)
                        : bn == 128 ? cluster_fits<128, 3, true, true, 2>(splits)
@@ -662,6 +686,11 @@ bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits) {
     return bn == 64    ? cluster_fits<64, 4, false, false>(splits)
            : bn == 128 ? cluster_fits<128, 3, false, false>(splits)
                        : bn == 256 && cluster_fits<256, 4, false, false>(splits);
+}
+
+int tc_wgrad_stages(int bn, int im2col, int kb1) {
+    if (im2col) return kb1 ? (bn == 128 ? 6 : 4) : (bn == 128 ? 3 : 2);
+    return bn == 128 ? 3 : 4;
 }
 
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,

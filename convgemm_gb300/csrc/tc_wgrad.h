@@ -23,6 +23,9 @@ struct TcWgradParams {
     // 2..8 splits as one thread-block cluster along z: the partial tiles meet in
     // distributed shared memory and the cluster writes dW (no workspace, no reduction launch)
     int cluster;
+    // im2col path: one 64-pixel chunk per ring stage and twice the stages (else two chunks
+    // per stage): the ring's stage count is a tuned choice
+    int kb1;
     // more splits than one cluster holds: `groups` clusters of `csize` splits per tile
     // (cluster dimension z = csize, splits = groups * csize).  Rank r of each cluster writes
     // its row slice of the cluster's sum to gws [tile][group][128][BN]; the last cluster to
@@ -36,8 +39,10 @@ struct TcWgradParams {
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                             int mtiles, int ntiles, int splits, cudaStream_t st);
-// Whether splits (2..8) can run as clusters for this tile width / operand side.
-bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits);
+// Whether splits (2..8) can run as clusters for this tile width / operand side / stage form.
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1 = 0);
+// Ring stages of the general weight-gradient kernel for a tile width and form.
+int tc_wgrad_stages(int bn, int im2col, int kb1);
 // Tile counters of the grouped cluster reduction on the current device: `n` consecutive
 // zero words for one launch (a rotating range of a fixed device array; NULL if unavailable).
 unsigned *tc_wgrad_counters(int n);

@@ -56,6 +56,18 @@ def dgrad_bf16_ex(shape: Shape, dy, wpacked, dx, relu_x=None, accumulate=False, 
                                            int(bool(accumulate)), _stream(stream)))
 
 
+def dgrad_bf16_bias_grad(shape: Shape, dy, wpacked, dx, db, relu_x=None, workspace=None, stream=None):
+    """Input gradient (masked by relu_x > 0 when given) with the column sums of dx fused into its
+    epilogue: db[ci] = sum over pixels of dx, the bias gradient of the layer that produced relu_x."""
+    import torch
+    n = lib().convgemm_dgrad_bf16_bias_grad_workspace_size(ctypes.byref(shape))
+    if workspace is None:
+        workspace = torch.empty(n // 4 + 4, device=dy.device)
+    _raise_if(lib().convgemm_dgrad_bf16_bias_grad(ctypes.byref(shape), ptr(dy), ptr(wpacked), ptr(dx), ptr(relu_x),
+                                                  ptr(db), ptr(workspace), workspace.numel() * workspace.element_size(),
+                                                  _stream(stream)))
+
+
 def bias_grad_bf16(shape: Shape, dy, db, workspace=None, stream=None):
     """db[co] = sum over output pixels of dy[p][co] (FP32, fixed order)."""
     import torch
@@ -111,6 +123,9 @@ def wgrad_bf16_plan(shape: Shape):
 TUNE_FWD, TUNE_DGRAD, TUNE_WGRAD, TUNE_FWD_FP8, TUNE_FWD_BF16X3 = range(5)
 WGRAD_X_ON_A = 0x10000      # weight-gradient aux flags: X as the A operand of a wide layer,
 WGRAD_IM2COL_X = 0x20000    # X of a 1x1 stride-1 unpadded layer by im2col instead of tiled boxes
+WGRAD_SLAB = 0x80000        # stride-1 layers with 128-channel blocks: the slab kernel
+WGRAD_STAGES1 = 0x400000    # im2col path: one chunk per ring stage, twice the stages
+CONV_STAGES1 = 16           # forward / input-gradient aux: one K block per ring stage, twice the stages
 
 
 def WGRAD_GROUPS(csize: int) -> int:
@@ -121,6 +136,14 @@ def WGRAD_GROUPS(csize: int) -> int:
 def tune_set(op: int, shape: Shape, bn: int = 0, splits: int = 0):
     """Overrides the tile heuristics for one operation on one shape (0, 0 removes the entry)."""
     _raise_if(lib().convgemm_tune_set(op, ctypes.byref(shape), bn, splits))
+
+
+def tune_describe(op: int, shape: Shape):
+    """(kernel, bn, stages, cluster) that the tuning entry or heuristic selects for op on shape:
+    kernel 0 general / 1 slab / 2 small-channel; stages 0 where buffers are sized at run time."""
+    v = [ctypes.c_int() for _ in range(4)]
+    _raise_if(lib().convgemm_tune_describe(op, ctypes.byref(shape), *[ctypes.byref(x) for x in v]))
+    return tuple(x.value for x in v)
 
 
 def tune_clear():

@@ -82,6 +82,10 @@ void convgemm_clear_error(void);
  * library, convgemm_wgrad_bf16_noalloc's included; it is a file-scope device
  * variable, so neither this call nor any kernel launch allocates for it. */
 convgemm_status_t convgemm_check_device(void *stream);
+/* Measurement of the FP32 FMA peak (no counterpart in the reference): launches one kernel of
+ * independent FMA chains on every SM (`iters` loop trips per thread) on `stream` and returns in
+ * *flops the FLOPs it performs; time it with events to get FLOP/s.  out: one device float. */
+convgemm_status_t convgemm_measure_ffma(int iters, float *out, double *flops, void *stream);
 
 /* ------------------------------------------------------- FP32 plain form */
 
@@ -251,7 +255,9 @@ enum {
  * the weight gradient (bits 0-15; 0 = heuristic) plus the CONVGEMM_WGRAD_* flags
  * below, or, for the BF16 forward / input gradient, the number of
  * 128-row M tiles (1 or 2) that share each weight tile, plus 4 for the kernel
- * form with eight epilogue warps (short-K layers; 0 = heuristic).
+ * form with eight epilogue warps (short-K layers; 0 = heuristic), plus 8 for the general
+ * kernel instead of a slab kernel, plus 16 for one K block per ring stage and twice the
+ * stages (64 / 128-wide tiles, one M tile, four epilogue warps).
  * bn = aux = 0 removes the entry.  Set the weight-gradient entry before querying
  * its workspace size.  Thread-safe. */
 convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int bn, int aux);
@@ -268,8 +274,26 @@ convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int b
  * each tile to arrive): CONVGEMM_WGRAD_GROUPS(2 / 4 / 8).  The split count is rounded up to
  * a multiple of the cluster size.  The sum order is fixed by the split count and cluster
  * size, so dW stays bit-reproducible. */
+/* Weight gradient of a stride-1 layer whose channels are multiples of 128 and kn >= 64 (filters
+ * 2..512/BN taps wide, output width + filter span <= 256): the slab kernel, whose MMAs read
+ * each kernel row's taps as row-shifted windows of one input slab per band of output rows.
+ * It is the default for such layers when the tuning table has no entry for the shape;
+ * with an entry it runs when the entry carries this flag (its split count in bits 0-15,
+ * 0 = heuristic). */
+#define CONVGEMM_WGRAD_SLAB 0x80000
+/* Weight gradient (im2col path): one 64-pixel chunk per ring stage and twice as many stages
+ * (4 / 6 / 4 for 64 / 128 / 256-wide tiles) instead of two chunks per stage (2 / 3 / 2). */
+#define CONVGEMM_WGRAD_STAGES1 0x400000
 #define CONVGEMM_WGRAD_GROUPS(csize) ((csize) == 8 ? 0x300000 : (csize) == 4 ? 0x200000 : (csize) == 2 ? 0x100000 : 0)
 void convgemm_tune_clear(void);
+/* What the tuning table (or the heuristic) selects for the forward, input gradient or weight
+ * gradient on one shape: *kernel 0 the general implicit GEMM, 1 a slab kernel, 2 the
+ * small-channel kernel; *bn the tile width; *stages the ring stages of the general kernels (0 for
+ * the slab and small-channel kernels, which size their buffers at run time); *cluster 1, or the
+ * thread-block cluster size of a weight gradient whose splits are reduced in a cluster.  The
+ * reference chooses its blocking once, from the BLIS context (src/gemm_blis.h:181-188). */
+convgemm_status_t convgemm_tune_describe(int op, const convgemm_shape_t *shape, int *kernel, int *bn, int *stages,
+                                         int *cluster);
 
 /* ----------------------------------------- grouped persistent forward launch */
 
@@ -323,6 +347,19 @@ convgemm_status_t convgemm_dgrad_bf16_relu(const convgemm_shape_t *shape, const 
  * where relu_x <= 0, after the sum.  dx must be 16-byte aligned when accumulating. */
 convgemm_status_t convgemm_dgrad_bf16_ex(const convgemm_shape_t *shape, const void *dy, const void *wpacked, void *dx,
                                          const void *relu_x, int accumulate, void *stream);
+
+/* Input gradient with the bias gradient of the previous layer fused into its epilogue (the
+ * training step of a conv + bias + ReLU layer): dx as convgemm_dgrad_bf16_ex (relu_x masks it,
+ * or NULL; overwritten), and db[ci] = sum over all pixels of the masked dx, taken from the
+ * FP32 accumulators and reduced in a fixed order (bit-reproducible).  dx is the gradient at
+ * the previous layer's pre-activation output, so db is that layer's bias gradient (the
+ * reference has no bias gradient: its epilogue is inference-only, src/im2row_nhwc.c:269-285).
+ * workspace: convgemm_dgrad_bf16_bias_grad_workspace_size bytes, 16-byte aligned.  Needs
+ * c % 8 == 0. */
+size_t convgemm_dgrad_bf16_bias_grad_workspace_size(const convgemm_shape_t *shape);
+convgemm_status_t convgemm_dgrad_bf16_bias_grad(const convgemm_shape_t *shape, const void *dy, const void *wpacked,
+                                                void *dx, const void *relu_x, float *db, void *workspace,
+                                                size_t workspace_bytes, void *stream);
 
 /* Bias gradient of the convolution: db[co] = sum over the b*ho*wo output pixels of
  * dy[p][co] (dy BF16 NHWC with kn rounded up to 8 channels, as for

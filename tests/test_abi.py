@@ -190,3 +190,30 @@ def test_weight_gradient_flags_in_plan_without_gpu(cglib):
         assert tc.wgrad_bf16_plan(s)[:2] == (256, 3)
     finally:
         tc.tune_clear()
+
+
+def test_shipped_tuning_table_entries_parse():
+    """Every tuned forward / input-gradient / weight-gradient entry of the shipped GB300 table
+    names its tile width, aux flags, kernel, ring stages and cluster size, within the ranges the
+    library accepts (convgemm_tune_set / convgemm_tune_describe)."""
+    import json
+    path = os.path.join(ROOT, "convgemm_gb300", "autotune_gb300.json")
+    table = json.load(open(path))["NVIDIA GB300"]
+    ops = [k for k in table if "|" in k and k.split("|")[0].split(".")[0] in ("fwd", "dgrad", "wgrad")]
+    assert len(ops) >= 100
+    for k in ops:
+        e = table[k]
+        op = k.split(".")[0]
+        assert e["bn"] in (0, 64, 128, 256), k
+        aux = int(e["splits"])
+        if op == "wgrad":
+            assert aux >= 0 and (aux & ~0x7BFFFF) == 0, k
+        else:
+            assert (aux & ~24) in (0, 1, 2, 5, 6), k
+        assert e["kernel"] in (0, 1, 2), k
+        assert e["stages"] in (0, 2, 3, 4, 6, 8), k
+        assert 1 <= e["cluster"] <= 8, k
+        if e["kernel"] == 0:
+            assert e["stages"] >= 2, k
+        shape = [int(v) for v in k.split("|")[1].split("x")]
+        assert len(shape) == 13 and min(shape[:7]) >= 1, k

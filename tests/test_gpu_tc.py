@@ -363,6 +363,112 @@ def test_wgrad_grouped_cluster_reduction(cglib, oracle_lib, b, h, w, c, kn, k, s
     assert cg.lib().convgemm_launch_count() > n0
 
 
+@pytest.mark.parametrize("b,h,w,c,kn,k,pad,dil,splits", [
+    (8, 28, 28, 128, 128, 3, 1, 1, 0),    # ResNet-50 stage 2 3x3: heuristic split count
+    (4, 14, 14, 256, 256, 3, 1, 1, 0),    # stage 3: two input-block pairs, two output tiles
+    (4, 7, 7, 512, 512, 3, 1, 1, 0),      # stage 4: one band per image
+    (2, 20, 18, 128, 96, 3, 1, 1, 5),     # kn = 96: partial output tile, W != H
+    (2, 16, 16, 124, 64, 3, 2, 2, 3),     # 124 channels padded to 128, 64-wide tile, dilation 2
+    (2, 12, 11, 128, 128, 2, 0, 1, 2),    # even filter, no padding
+    (1, 9, 9, 256, 128, 3, 1, 1, 1),      # one split: dW written by the kernel
+])
+def test_wgrad_slab_kernel(cglib, oracle_lib, b, h, w, c, kn, k, pad, dil, splits):
+    """The slab weight gradient (stride 1, 128-channel input blocks): within FP32 accumulation of
+    FP64 on the same BF16 inputs in both dW layouts, bit-reproducible, and within the same bound
+    of the general kernel's result."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, 1, 1, dil, dil)
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, dil=dil)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(91 + c + kn + k)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * ho * wo * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, ho, wo)
+    ref = O.wgrad_f64(C.NHWC, g, bf16r(dy), bf16r(x))
+    ref_nchw = O.wgrad_f64(C.NCHW, g, np.ascontiguousarray(bf16r(dy).reshape(b, ho, wo, kn).transpose(0, 3, 1, 2)).ravel(),
+                           np.ascontiguousarray(bf16r(x).reshape(b, h, w, c).transpose(0, 3, 1, 2)).ravel())
+    K = c * k * k
+
+    def run(bn, aux, layout):
+        tc.tune_set(tc.TUNE_WGRAD, s, bn, aux)
+        ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+        d = torch.full((K * kn,), float("nan"), device="cuda")
+        tc.wgrad_bf16(layout, s, dyd, xd, d, ws)
+        torch.cuda.synchronize()
+        cg.check_device()
+        return d
+
+    try:
+        aux = tc.WGRAD_SLAB | splits
+        d0 = run(0, aux, cg.NHWC)
+        if splits:   # at most the requested split count (whole bands per split)
+            assert 1 <= tc.wgrad_bf16_plan(s)[1] <= splits
+        d1 = run(0, aux, cg.NHWC)
+        assert torch.equal(d0, d1), "bit-reproducible"
+        assert rel_max_rms(d0.cpu().numpy(), ref)[0] <= 1e-4
+        dn = run(0, aux, cg.NCHW)
+        assert rel_max_rms(dn.cpu().numpy(), ref_nchw)[0] <= 1e-4
+        general = run(128 if kn > 64 else 64, 4, cg.NHWC)
+        assert rel_max_rms(general.cpu().numpy(), ref)[0] <= 1e-4
+    finally:
+        tc.tune_clear()
+
+
+def test_ring_stage_forms_give_identical_results(cglib):
+    """The tuned ring-stage forms (one K block or one 64-pixel chunk per stage, twice the stages)
+    issue the same MMAs in the same order: forward, input gradient and weight gradient are bit-
+    identical to the default forms, and tune_describe reports the stage count of each form."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    b, h, w, c, kn = 4, 14, 14, 128, 128
+    s = cg.Shape.of(b, h, w, c, kn, 3, 3, 1, 1)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    wt = (rng.standard_normal(9 * c * kn) * np.sqrt(2.0 / (9 * c))).astype(np.float32)
+    dy = rng.standard_normal(b * h * w * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, h, w)
+    wp = pack(cg, tc, s, tc.OPERAND_FWD, wt)
+    wpd = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    try:
+        outs = {}
+        for bn in (64, 128):
+            for aux in (1, 1 | tc.CONV_STAGES1):
+                tc.tune_set(tc.TUNE_FWD, s, bn, aux)
+                tc.tune_set(tc.TUNE_DGRAD, s, bn, aux)
+                kern, bnd, stages, cl = tc.tune_describe(tc.TUNE_FWD, s)
+                assert (kern, bnd, cl) == (0, bn, 1)
+                assert stages == {64: 4, 128: 3}[bn] * (2 if aux & tc.CONV_STAGES1 else 1)
+                y = torch.empty(b, h, w, kn, dtype=torch.bfloat16, device="cuda")
+                dx = torch.empty(b, h, w, c, dtype=torch.bfloat16, device="cuda")
+                tc.fwd_bf16(s, xd, wp, y)
+                tc.dgrad_bf16(s, dyd, wpd, dx)
+                outs[(bn, aux)] = (y, dx)
+        torch.cuda.synchronize()
+        cg.check_device()
+        ref_y, ref_dx = outs[(64, 1)]
+        for y, dx in outs.values():
+            assert torch.equal(y, ref_y) and torch.equal(dx, ref_dx)
+        for bn, splits in ((128, 4), (256, 3), (64, 12)):
+            dws = []
+            for flag in (0, tc.WGRAD_STAGES1):
+                tc.tune_set(tc.TUNE_WGRAD, s, bn, splits | tc.WGRAD_X_ON_A * (bn != 64) | flag)
+                kern, bnd, stages, cl = tc.tune_describe(tc.TUNE_WGRAD, s)
+                assert kern == 0 and bnd == bn
+                assert stages == {64: 2, 128: 3, 256: 2}[bn] * (2 if flag else 1)
+                ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+                d = torch.empty(9 * c * kn, device="cuda")
+                tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d, ws)
+                dws.append(d)
+            torch.cuda.synchronize()
+            cg.check_device()
+            assert torch.equal(dws[0], dws[1]), (bn, splits)
+    finally:
+        tc.tune_clear()
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc
@@ -531,6 +637,49 @@ def test_bias_grad_against_fp64(cglib, shape):
     assert torch.equal(db1, db2)
     ref = bf16r(dy).astype(np.float64).reshape(-1, kn).sum(0)
     assert np.abs(db1.cpu().numpy() - ref).max() <= 1e-5 * np.abs(bf16r(dy)).reshape(-1, kn).sum(0).max()
+
+
+BGRAD_SHAPES = [(4, 14, 14, 64, 128, 3, 1, 1, 1),    # stride 1, one stride-phase class
+                (2, 14, 14, 128, 64, 1, 0, 2, 1),    # 1x1/s2: three classes receive no tap (zero, nothing summed)
+                (2, 9, 9, 64, 96, 3, 1, 2, 1),       # four stride-phase classes
+                (1, 12, 10, 32, 48, 3, 2, 1, 2)]     # ragged channels: cp.async gather path, dilation 2
+
+
+@pytest.mark.parametrize("shape", BGRAD_SHAPES, ids=str)
+@pytest.mark.parametrize("masked", [False, True], ids=["plain", "relu"])
+def test_dgrad_with_fused_bias_grad(cglib, oracle_lib, shape, masked):
+    """convgemm_dgrad_bf16_bias_grad: dx bit-identical to the input gradient of
+    convgemm_dgrad_bf16_ex (same mask), and db = the per-channel sum of the masked input gradient
+    within FP32 accumulation of the FP64 oracle's, bit-reproducible run to run."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    b, h, w, c, kn, k, pad, stride, dil = shape
+    g = C.geom(b, h, w, c, kn, k, k, pad=pad, stride=stride, dil=dil)
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, stride, stride, dil, dil)
+    rng = np.random.default_rng(41 + sum(shape))
+    K = c * k * k
+    wt = (rng.standard_normal(K * kn) * np.sqrt(2.0 / K)).astype(np.float32)
+    dy = rng.standard_normal(b * s.ho * s.wo * kn).astype(np.float32)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, s.ho, s.wo)
+    wp = pack(cg, tc, s, tc.OPERAND_DGRAD, wt)
+    x = (torch.rand(b, h, w, c, device="cuda") - 0.3).to(torch.bfloat16) if masked else None
+    dx = torch.full((b, h, w, c), float("nan"), dtype=torch.bfloat16, device="cuda")
+    db1, db2 = torch.empty(c, device="cuda"), torch.empty(c, device="cuda")
+    tc.dgrad_bf16_bias_grad(s, dyd, wp, dx, db1, relu_x=x)
+    dx2 = torch.empty_like(dx)
+    tc.dgrad_bf16_bias_grad(s, dyd, wp, dx2, db2, relu_x=x)
+    want = torch.full_like(dx, float("nan"))
+    tc.dgrad_bf16_ex(s, dyd, wp, want, relu_x=x)
+    torch.cuda.synchronize()
+    cg.check_device()
+    assert torch.equal(dx.view(torch.int16), want.view(torch.int16))
+    assert torch.equal(db1, db2) and torch.equal(dx, dx2)
+    ref = O.dgrad_f64(C.NHWC, g, bf16r(wt), bf16r(dy)).reshape(-1, c)
+    if masked:
+        ref = np.where(x.float().cpu().numpy().reshape(-1, c) > 0, ref, 0.0)
+    want_db = ref.sum(0)
+    got = db1.cpu().numpy().astype(np.float64)
+    assert np.abs(got - want_db).max() <= 1e-5 * np.abs(ref).sum(0).max()
 
 
 SLAB_SHAPES = [
