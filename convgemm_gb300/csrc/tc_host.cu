@@ -638,6 +638,7 @@ struct WgPlan {
     int csize, groups;   // grouped cluster reduction (groups > 1): splits = groups * csize
     int slab;            // the slab kernel (tc_wgrad_slab.cu) with `splits` partials
     int kb1;             // im2col path: one chunk per ring stage (twice the stages)
+    int iss2;            // im2col path, two chunks per stage: two MMA-issuing warps
     size_t ws_bytes;
 };
 
@@ -661,6 +662,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     const bool im2col = wgrad_im2col_ok(s, g);
     const int aux_splits = t.splits & 0xffff;
     w.kb1 = im2col && (t.splits & CONVGEMM_WGRAD_STAGES1) ? 1 : 0;
+    w.iss2 = im2col && !w.kb1 && (t.splits & CONVGEMM_WGRAD_TWO_ISSUERS) ? 1 : 0;
     // X on the A side: always for narrow layers, on request for wide ones (im2col path)
     const bool x_on_a = (t.splits & CONVGEMM_WGRAD_X_ON_A) && im2col;
     w.xa = s.kn < 128 || x_on_a;
@@ -720,7 +722,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         if (grouped > w.ws_bytes) w.ws_bytes = grouped;
         const int code = (t.splits >> 20) & 3;   // CONVGEMM_WGRAD_GROUPS: 1, 2, 3 -> clusters of 2, 4, 8
         const int want = code ? 1 << code : 0;
-        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want, w.kb1) ? want : 0;
+        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want, w.kb1, w.iss2) ? want : 0;
         if (cs) {
             w.csize = cs;
             w.groups = (w.splits + cs - 1) / cs;
@@ -825,6 +827,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.layout = layout == CONVGEMM_NCHW;
     p.C = s.c;
     p.kb1 = w.kb1;
+    p.iss2 = w.iss2;
     if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
         // clusters of csize splits; the tile's last cluster adds the clusters' sums
         p.cluster = 1;
@@ -834,7 +837,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         p.counters = tc_wgrad_counters(w.mtiles * w.ntiles * w.csize);
         if (!p.counters) return cg_set_error(CONVGEMM_ERROR_CUDA, "convgemm_wgrad_bf16: tile counters unavailable");
     } else {
-        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1);
+        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1, w.iss2);
     }
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
@@ -872,7 +875,7 @@ extern "C" convgemm_status_t convgemm_tune_describe(int op, const convgemm_shape
         const int im2col = wgrad_im2col_ok(s, g);
         *stages = tc_wgrad_stages(w.bn, im2col, w.kb1);
         if (w.groups > 1) *cluster = w.csize;
-        else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1)) *cluster = w.splits;
+        else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1, w.iss2)) *cluster = w.splits;
         return CONVGEMM_SUCCESS;
     }
     if (op != CONVGEMM_TUNE_FWD && op != CONVGEMM_TUNE_DGRAD)

@@ -52,17 +52,24 @@ struct WgCfg {
 // Warps: the gather warps (one TMA-issuing thread on the im2col path; eight warps of
 // cp.async gathers otherwise, whose issue rate bounds that path), then the MMA warp;
 // warps 0-3 run the epilogue.
-template <bool IM2C>
+// ISS2: a second MMA-issuing warp (warp GW + 1).  Each issuer takes alternate chunks of every
+// two-chunk stage into its own accumulator and the epilogue adds the two: one thread's tcgen05
+// issue, barrier wait and commit cost tens of cycles each, which bounds a single issuer of the
+// eight 128-wide MMAs of a stage.
+template <bool IM2C, bool ISS2 = false>
 struct WgWarps {
-    static constexpr int GW = IM2C ? 4 : 8, THREADS = 32 * (GW + 1);
+    static constexpr int GW = IM2C ? 4 : 8, THREADS = 32 * (GW + 1 + (ISS2 ? 1 : 0));
 };
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB>
-__global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
+template <int BN, int STAGES, bool XA, bool IM2C, int KB, bool ISS2 = false>
+__global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
                     const __grid_constant__ CUtensorMap xmap) {
     using C = WgCfg<BN, STAGES, XA, KB>;
     static_assert(IM2C || KB == 1, "the cp.async gather fills one chunk per stage");
+    static_assert(!ISS2 || (IM2C && KB == 2), "two issuers: alternate chunks of two-chunk stages");
+    constexpr uint32_t NISS = ISS2 ? 2 : 1;
+    constexpr uint32_t TCOLS = ISS2 ? 2 * BN : BN;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *base = (uint8_t *) (((uintptr_t) smem_raw + 1023) & ~(uintptr_t) 1023);
     uint64_t *full = (uint64_t *) (base + STAGES * C::STAGE_BYTES);
@@ -75,15 +82,15 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             tc::mbar_init(&full[s], IM2C ? 1 : 32 * GW + 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], NISS);
         }
-        tc::mbar_init(accum, 1);
+        tc::mbar_init(accum, NISS);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&dymap);
         if (IM2C) tc::prefetch_tmap(&xmap);
     }
     if (warp == GW) {
-        tc::tmem_alloc(tmem_holder, BN);
+        tc::tmem_alloc(tmem_holder, TCOLS);
         tc::tmem_relinquish();
     }
     tc::pdl_wait();   // no global memory access above
@@ -219,6 +226,20 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
         // epilogue: FP32 partial tile -> workspace [split][Mext][Next]
         if (ok) ok = tc::mbar_wait(accum, 0, p.err, 13);
         tc::tc_fence_after();
+        // 32 columns of this warp's rows: the accumulator, plus the second issuer's (odd chunks)
+        auto ld_acc = [&](int c0, uint32_t(&v)[32]) {
+            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+            tc::tmem_ld_wait();
+            if constexpr (ISS2) {
+                if (KT >= 2) {
+                    uint32_t u[32];
+                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) (BN + c0), u);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int i = 0; i < 32; i++) v[i] = __float_as_uint(__fadd_rn(__uint_as_float(v[i]), __uint_as_float(u[i])));
+                }
+            }
+        };
         const int m = mrow0 + warp * 32 + lane;
         const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx;
         float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
@@ -230,8 +251,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t v[32];
                 if (ok && KT > 0) {   // a split past the last chunk (grouped clusters) adds zero
-                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
-                    tc::tmem_ld_wait();
+                    ld_acc(c0, v);
                 } else {
 #pragma unroll
                     for (int jj = 0; jj < 32; jj++) v[jj] = 0u;
@@ -248,8 +268,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t v[32];
-                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
-                tc::tmem_ld_wait();
+                ld_acc(c0, v);
                 if (m >= Mext) continue;
 #pragma unroll 4
                 for (int jj = 0; jj < 32; jj++) {
@@ -268,8 +287,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
                 uint32_t v[32];
-                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
-                tc::tmem_ld_wait();
+                ld_acc(c0, v);
                 const int nb = ncol0 + c0;
                 if (m < Mext && nb < Next) {
                     if (nb + 32 <= Next && (Next & 3) == 0) {
@@ -286,9 +304,11 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
                 }
             }
         }
-    } else if (warp == GW) {
+    } else if (warp == GW || (ISS2 && warp == GW + 1)) {
         if (lane == 0) {
             constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
+            const int j = warp - GW;   // issuer: chunk parity it takes (ISS2), accumulator
+            const uint32_t dt = tmem + (uint32_t) (j * BN);
             for (int g = 0; g < NG; g++) {
                 const int s = g % STAGES;
                 const uint32_t ph = (g / STAGES) & 1;
@@ -303,10 +323,11 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
 #pragma unroll
                 for (int c = 0; c < KB; c++) {
                     if (c >= nch) break;
+                    if (ISS2 && c != j) continue;
                     const uint64_t ad = ad0 + ((c * C::CHUNK_BYTES) >> 4), bd = ad + (C::A_BYTES >> 4);
 #pragma unroll
                     for (int k = 0; k < C::BK / 16; k++)
-                        tc::mma_f16(tmem, ad + 128 * k, bd + 128 * k, idesc, (g | c | k) != 0);
+                        tc::mma_f16(dt, ad + 128 * k, bd + 128 * k, idesc, (g | (ISS2 ? 0 : c) | k) != 0);
                 }
                 tc::mma_commit(&empty[s]);
             }
@@ -427,7 +448,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C>::THREADS, 1)
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == GW) tc::tmem_dealloc(tmem, BN);
+    if (warp == GW) tc::tmem_dealloc(tmem, TCOLS);
 }
 
 // First pass of the reduction when there are many splits: group g sums the
@@ -514,11 +535,11 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false>
 cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUtensorMap &xmap, dim3 grid,
                       cudaStream_t st) {
     using C = WgCfg<BN, STAGES, XA, KB>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -528,7 +549,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     // Weight-gradient work runs beside the forward / input-gradient chain on a side
     // stream: launched without programmatic serialization, so that its grids do not
     // hold SMs early while the persistent chain kernels want them.
-    constexpr int THREADS = WgWarps<IM2C>::THREADS;
+    constexpr int THREADS = WgWarps<IM2C, ISS2>::THREADS;
     if (!p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(THREADS), C::SMEM, st, p, map, xmap);
     // the splits of one tile as a cluster along z
     cudaLaunchConfig_t cfg = {};
@@ -548,10 +569,10 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
 }
 
 // Whether `splits` CTAs of this configuration can be resident together as one cluster.
-template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false>
 bool cluster_fits(int splits) {
     using C = WgCfg<BN, STAGES, XA, KB>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2>;
     static int cached[9] = {-1, -1, -1, -1, -1, -1, -1, -1, -1};
     if (splits < 2 || splits > 8) return false;
     if (cached[splits] < 0) {
@@ -561,7 +582,7 @@ bool cluster_fits(int splits) {
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(1, 1, splits);
-        cfg.blockDim = dim3(WgWarps<IM2C>::THREADS);
+        cfg.blockDim = dim3(WgWarps<IM2C, ISS2>::THREADS);
         cfg.dynamicSmemBytes = C::SMEM;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -599,6 +620,22 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
                 case 64: return launch_wg<64, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
                 case 128: return launch_wg<128, 6, false, IM2C, 1>(p, dymap, xmap, grid, st);
                 case 256: return launch_wg<256, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        if (p.iss2) {   // two MMA issuers on the two-chunk stages
+            if (xa) {
+                switch (bn) {
+                    case 64: return launch_wg<64, 2, true, IM2C, 2, true>(p, dymap, xmap, grid, st);
+                    case 128: return launch_wg<128, 3, true, IM2C, 2, true>(p, dymap, xmap, grid, st);
+                    case 256: return launch_wg<256, 2, true, IM2C, 2, true>(p, dymap, xmap, grid, st);
+                    default: return cudaErrorInvalidValue;
+                }
+            }
+            switch (bn) {
+                case 64: return launch_wg<64, 2, false, IM2C, 2, true>(p, dymap, xmap, grid, st);
+                case 128: return launch_wg<128, 3, false, IM2C, 2, true>(p, dymap, xmap, grid, st);
+                case 256: return launch_wg<256, 2, false, IM2C, 2, true>(p, dymap, xmap, grid, st);
                 default: return cudaErrorInvalidValue;
             }
         }
@@ -664,8 +701,16 @@ unsigned *tc_wgrad_counters(int n) {
     return r;
 }
 
-bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1) {
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1, int iss2) {
     if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;
+    if (im2col && iss2 && !kb1) {
+        if (xa) return bn == 64    ? cluster_fits<64, 2, true, true, 2, true>(splits)
+                       : bn == 128 ? cluster_fits<128, 3, true, true, 2, true>(splits)
+                                   : bn == 256 && cluster_fits<256, 2, true, true, 2, true>(splits);
+        return bn == 64    ? cluster_fits<64, 2, false, true, 2, true>(splits)
+               : bn == 128 ? cluster_fits<128, 3, false, true, 2, true>(splits)
+                           : bn == 256 && cluster_fits<256, 2, false, true, 2, true>(splits);
+    }
     if (im2col && kb1) {
         if (xa) return bn == 64    ? cluster_fits<64, 4, true, true, 1>(splits)
                        : bn == 128 ? cluster_fits<128, 6, true, true, 1>(splits)

@@ -284,6 +284,10 @@ convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int b
 /* Weight gradient (im2col path): one 64-pixel chunk per ring stage and twice as many stages
  * (4 / 6 / 4 for 64 / 128 / 256-wide tiles) instead of two chunks per stage (2 / 3 / 2). */
 #define CONVGEMM_WGRAD_STAGES1 0x400000
+/* Weight gradient (im2col path, two chunks per stage): a second MMA-issuing warp takes the odd
+ * chunks into a second accumulator, added in the epilogue (another summation order: results
+ * stay within the FP32 accumulation bound and bit-reproducible). */
+#define CONVGEMM_WGRAD_TWO_ISSUERS 0x800000
 #define CONVGEMM_WGRAD_GROUPS(csize) ((csize) == 8 ? 0x300000 : (csize) == 4 ? 0x200000 : (csize) == 2 ? 0x100000 : 0)
 void convgemm_tune_clear(void);
 /* What the tuning table (or the heuristic) selects for the forward, input gradient or weight

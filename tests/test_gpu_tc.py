@@ -100,6 +100,8 @@ DGRAD_SHAPES = [
     (1, 12, 10, 32, 48, 3, 2, 1, 2),
     (3, 7, 7, 512, 512, 3, 1, 1, 1),
     (2, 9, 9, 128, 64, 3, 0, 2, 1),      # no padding, odd size
+    (2, 7, 9, 64, 128, 1, 0, 2, 1),      # 1x1/s2, odd sizes: the unreached pixels are zero
+    (1, 12, 12, 128, 64, 1, 0, 3, 1),    # 1x1/s3: eight zero pixels per reached one
 ]
 
 
@@ -465,6 +467,19 @@ def test_ring_stage_forms_give_identical_results(cglib):
             torch.cuda.synchronize()
             cg.check_device()
             assert torch.equal(dws[0], dws[1]), (bn, splits)
+            # two MMA issuers (odd chunks into a second accumulator): another FP32 summation order,
+            # reproducible and within FP32 accumulation of the one-issuer result
+            two = []
+            for _ in range(2):
+                tc.tune_set(tc.TUNE_WGRAD, s, bn, splits | tc.WGRAD_X_ON_A * (bn != 64) | tc.WGRAD_TWO_ISSUERS)
+                ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+                d = torch.empty(9 * c * kn, device="cuda")
+                tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d, ws)
+                two.append(d)
+            torch.cuda.synchronize()
+            cg.check_device()
+            assert torch.equal(two[0], two[1]), (bn, splits)
+            assert ((two[0] - dws[0]).abs().max() / dws[0].abs().max()).item() <= 1e-5, (bn, splits)
     finally:
         tc.tune_clear()
 
