@@ -531,6 +531,29 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                         bulk_commit();
                     }
                     if (C::EPI_BUFS == 2) ebuf ^= 1;
+                } else if (!C::OUTF32 && nb + C::CW <= p.Cout && __any_sync(0xFFFFFFFFu, orow != nullptr)) {
+                    // rows scattered over the output (stride-phase classes): staged through this warp's
+                    // buffer, then each store instruction writes four whole 128-byte rows (eight lanes
+                    // per row) instead of 16 bytes of 32 rows
+                    uint8_t *stg = stg_warp + ebuf * C::EPI_BYTES;
+                    if (lane == 0 && C::EPI_BUFS == 2) bulk_wait_read<1>();
+                    else if (lane == 0) bulk_wait_read<0>();
+                    __syncwarp();
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+                        *reinterpret_cast<uint4 *>(stg + lane * 128 + ((q ^ (lane & 7)) << 4)) =
+                            make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+                    __syncwarp();
+                    const unsigned long long my = (unsigned long long) (orow ? orow + (size_t) nb * 2 : nullptr);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        const int r = q * 4 + (lane >> 3), ch = lane & 7;
+                        const unsigned long long dst = __shfl_sync(0xFFFFFFFFu, my, r);
+                        const uint4 u = *reinterpret_cast<const uint4 *>(stg + r * 128 + ((ch ^ (r & 7)) << 4));
+                        if (dst) *reinterpret_cast<uint4 *>((uint8_t *) dst + ch * 16) = u;
+                    }
+                    __syncwarp();
+                    if (C::EPI_BUFS == 2) ebuf ^= 1;
                 } else if (orow && nb < p.Cout) {
                     if (nb + C::CW <= p.Cout) {
                         uint4 *dst = reinterpret_cast<uint4 *>(orow + (size_t) nb * (C::OUTF32 ? 4 : 2));
