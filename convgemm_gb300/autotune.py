@@ -30,7 +30,7 @@ from . import tc
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
 OP_CACHE_TAG = "v6"   # op entries: fwd / dgrad with the M-tile, epilogue-warp and ring-stage choices
-WGRAD_CACHE_TAG = "v9"   # wgrad: ring stages, two issuers, direct single-split writes, 2..8-split clusters, grouped clusters, slab kernel
+WGRAD_CACHE_TAG = "v10"   # wgrad: ring stages, two issuers, 128-pixel chunks, direct single-split writes, 2..8-split clusters, grouped clusters, slab kernel
 
 
 def cache_path() -> str:
@@ -219,10 +219,12 @@ def op_candidates(op: int, s):
     # ring (im2col path), for every tile and split
     if tc.c8(s.c) % 64 == 0:
         base = list(out)
-        out += [(w, sp | tc.WGRAD_STAGES1) for w, sp in base] + [(w, sp | tc.WGRAD_TWO_ISSUERS) for w, sp in base]
+        out += [(w, sp | tc.WGRAD_STAGES1) for w, sp in base] + [(w, sp | tc.WGRAD_TWO_ISSUERS) for w, sp in base] + \
+            [(w, sp | tc.WGRAD_WIDE_CHUNKS) for w, sp in base]
     # more than 8 splits: also the in-kernel reduction by clusters of 2 / 4 / 8 splits
     out += [(w, sp | tc.WGRAD_GROUPS(cs)) for w, sp in list(out)
-            if (sp & 0xffff) > 8 and not sp & (tc.WGRAD_STAGES1 | tc.WGRAD_TWO_ISSUERS) for cs in (2, 4, 8)]
+            if (sp & 0xffff) > 8 and not sp & (tc.WGRAD_STAGES1 | tc.WGRAD_TWO_ISSUERS | tc.WGRAD_WIDE_CHUNKS)
+            for cs in (2, 4, 8)]
     # stride-1 layers with 128-channel blocks: the slab kernel around its own split heuristic
     tc.tune_set(op, s, 0, tc.WGRAD_SLAB)
     bn_s, s3, _ = tc.wgrad_bf16_plan(s)

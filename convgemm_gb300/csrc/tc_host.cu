@@ -639,6 +639,8 @@ struct WgPlan {
     int slab;            // the slab kernel (tc_wgrad_slab.cu) with `splits` partials
     int kb1;             // im2col path: one chunk per ring stage (twice the stages)
     int iss2;            // im2col path, two chunks per stage: two MMA-issuing warps
+    int wide;            // im2col path: 128-pixel chunks (twice the bytes per TMA box), one per stage
+    int bk;              // pixels per chunk (64, or 128 when wide)
     size_t ws_bytes;
 };
 
@@ -661,8 +663,10 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.Nx = s.kh * s.kw * w.Cp;
     const bool im2col = wgrad_im2col_ok(s, g);
     const int aux_splits = t.splits & 0xffff;
-    w.kb1 = im2col && (t.splits & CONVGEMM_WGRAD_STAGES1) ? 1 : 0;
-    w.iss2 = im2col && !w.kb1 && (t.splits & CONVGEMM_WGRAD_TWO_ISSUERS) ? 1 : 0;
+    w.wide = im2col && (t.splits & CONVGEMM_WGRAD_WIDE_CHUNKS) ? 1 : 0;
+    w.kb1 = im2col && !w.wide && (t.splits & CONVGEMM_WGRAD_STAGES1) ? 1 : 0;
+    w.iss2 = im2col && !w.kb1 && !w.wide && (t.splits & CONVGEMM_WGRAD_TWO_ISSUERS) ? 1 : 0;
+    w.bk = w.wide ? 128 : 64;
     // X on the A side: always for narrow layers, on request for wide ones (im2col path)
     const bool x_on_a = (t.splits & CONVGEMM_WGRAD_X_ON_A) && im2col;
     w.xa = s.kn < 128 || x_on_a;
@@ -683,11 +687,11 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     }
     w.mtiles = (Mext + 127) / 128;
     w.ntiles = (Next + w.bn - 1) / w.bn;
-    w.nchunks = (int) ((g.P + 63) / 64);
+    w.nchunks = (int) ((g.P + w.bk - 1) / w.bk);
     const int base = w.mtiles * w.ntiles;
     const int per_sm = w.bn == 256 ? 1 : 2;
     int splits = tc_num_sms() * per_sm / base;   // one wave: no partial second wave
-    const int max_splits = (w.nchunks + 7) / 8;  // at least 8 chunks (512 pixels) per split
+    const int max_splits = (int) ((g.P + 511) / 512);   // at least 512 pixels per split
     if (splits > max_splits) splits = max_splits;
     if (aux_splits) splits = aux_splits < w.nchunks ? aux_splits : w.nchunks;
     if (splits < 1) splits = 1;
@@ -722,7 +726,7 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         if (grouped > w.ws_bytes) w.ws_bytes = grouped;
         const int code = (t.splits >> 20) & 3;   // CONVGEMM_WGRAD_GROUPS: 1, 2, 3 -> clusters of 2, 4, 8
         const int want = code ? 1 << code : 0;
-        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want, w.kb1, w.iss2) ? want : 0;
+        const int cs = want && cg_wgrad_cluster_enabled() && tc_wgrad_cluster_ok(w.bn, w.xa, im2col, want, w.kb1, w.iss2, w.wide) ? want : 0;
         if (cs) {
             w.csize = cs;
             w.groups = (w.splits + cs - 1) / cs;
@@ -777,7 +781,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
                                  layout == CONVGEMM_NCHW, (cudaStream_t) stream);
     }
     CUtensorMap map;
-    if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, w.kn8, 64, 64))
+    if (convgemm_status_t e = tc_make_map_2d(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, dy, g.P, w.kn8, 64, w.bk))
         return e;
     TcWgradParams p;
     memset(&p, 0, sizeof(p));
@@ -812,11 +816,11 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         p.im2col = wgrad_im2col_ok(s, g);
         p.x2d = w.x2d;
         if (p.x2d) {
-            if (convgemm_status_t e = tc_make_map_2d(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, x, g.P, p.Cp, 64, 64))
+            if (convgemm_status_t e = tc_make_map_2d(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, x, g.P, p.Cp, 64, w.bk))
                 return e;
         } else if (p.im2col) {
             if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
-                                                         s.vstride, s.hstride, 64, 2))
+                                                         s.vstride, s.hstride, w.bk, 2))
                 return e;
         }
     }
@@ -828,6 +832,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.C = s.c;
     p.kb1 = w.kb1;
     p.iss2 = w.iss2;
+    p.wide = w.wide;
     if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
         // clusters of csize splits; the tile's last cluster adds the clusters' sums
         p.cluster = 1;
@@ -837,7 +842,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         p.counters = tc_wgrad_counters(w.mtiles * w.ntiles * w.csize);
         if (!p.counters) return cg_set_error(CONVGEMM_ERROR_CUDA, "convgemm_wgrad_bf16: tile counters unavailable");
     } else {
-        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1, w.iss2);
+        p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1, w.iss2, w.wide);
     }
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))
@@ -873,9 +878,9 @@ extern "C" convgemm_status_t convgemm_tune_describe(int op, const convgemm_shape
         }
         const ConvGeom g = make_geom(s);
         const int im2col = wgrad_im2col_ok(s, g);
-        *stages = tc_wgrad_stages(w.bn, im2col, w.kb1);
+        *stages = tc_wgrad_stages(w.bn, im2col, w.kb1, w.wide);
         if (w.groups > 1) *cluster = w.csize;
-        else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1, w.iss2)) *cluster = w.splits;
+        else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1, w.iss2, w.wide)) *cluster = w.splits;
         return CONVGEMM_SUCCESS;
     }
     if (op != CONVGEMM_TUNE_FWD && op != CONVGEMM_TUNE_DGRAD)

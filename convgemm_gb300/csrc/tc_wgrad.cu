@@ -35,16 +35,17 @@ using bf16 = __nv_bfloat16;
 // KB chunks of BK pixels per pipeline stage: one full barrier and one MMA commit
 // cover KB chunks (the barrier round trip, not the loads or the MMAs, bounds a
 // one-chunk stage).
-template <int BN, int STAGES, bool XA, int KB = 1>
+template <int BN, int STAGES, bool XA, int KB = 1, int BKP = 64>
 struct WgCfg {
-    static constexpr int BM = 128, BK = 64;  // BK pixels per chunk
+    static constexpr int BM = 128, BK = BKP;  // BK pixels per chunk (64, or 128: each TMA box twice as large)
+    static constexpr uint32_t ATOM_BYTES = (uint32_t) BK * 128;   // 64 channels x BK pixels
     static constexpr uint32_t A_BYTES = BM * BK * 2;
     static constexpr uint32_t B_BYTES = BN * BK * 2;
     static constexpr uint32_t CHUNK_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t STAGE_BYTES = KB * CHUNK_BYTES;
     static constexpr int X_ATOMS = (XA ? BM : BN) / 64;    // 64-channel atoms gathered from X
     static constexpr int DY_ATOMS = (XA ? BN : BM) / 64;   // 64-channel atoms loaded from dY
-    static constexpr uint32_t DY_BYTES = DY_ATOMS * 64 * BK * 2;
+    static constexpr uint32_t DY_BYTES = DY_ATOMS * ATOM_BYTES;
     static constexpr int LAG = STAGES / 2;  // half the ring in flight, half queued for the MMA
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
 };
@@ -61,11 +62,12 @@ struct WgWarps {
     static constexpr int GW = IM2C ? 4 : 8, THREADS = 32 * (GW + 1 + (ISS2 ? 1 : 0));
 };
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB, bool ISS2 = false>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB, bool ISS2 = false, int BKP = 64>
 __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
                     const __grid_constant__ CUtensorMap xmap) {
-    using C = WgCfg<BN, STAGES, XA, KB>;
+    using C = WgCfg<BN, STAGES, XA, KB, BKP>;
+    static_assert(BKP == 64 || (IM2C && KB == 1 && !ISS2), "128-pixel chunks: im2col path, one chunk per stage");
     static_assert(IM2C || KB == 1, "the cp.async gather fills one chunk per stage");
     static_assert(!ISS2 || (IM2C && KB == 2), "two issuers: alternate chunks of two-chunk stages");
     constexpr uint32_t NISS = ISS2 ? 2 : 1;
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                 const uint32_t ph = (g / STAGES) & 1;
                 if (g >= STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11))) break;
                 const int nch = min(KB, KT - g * KB);
-                tc::mbar_arrive_expect_tx(&full[s], nch * (C::X_ATOMS * 8192 + C::DY_BYTES));
+                tc::mbar_arrive_expect_tx(&full[s], nch * (C::X_ATOMS * C::ATOM_BYTES + C::DY_BYTES));
                 for (int c = 0; c < nch; c++) {
                     const int pbase = (chunk0 + g * KB + c) * C::BK;
                     uint32_t q, ow, oh, b;
@@ -142,14 +144,14 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
 #pragma unroll
                     for (int a = 0; a < C::X_ATOMS; a++) {
                         if (p.x2d)   // one tap: the atom's channels are columns a_ci of the [P][Cp] matrix
-                            tc::tma_load_2d(st0 + xoff + a * 8192, &xmap, a_ci[a], pbase, &full[s]);
+                            tc::tma_load_2d(st0 + xoff + a * C::ATOM_BYTES, &xmap, a_ci[a], pbase, &full[s]);
                         else
-                            tc::tma_load_im2col_4d(st0 + xoff + a * 8192, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
+                            tc::tma_load_im2col_4d(st0 + xoff + a * C::ATOM_BYTES, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
                                                    a_oy[a], &full[s]);
                     }
 #pragma unroll
                     for (int a = 0; a < C::DY_ATOMS; a++)
-                        tc::tma_load_2d(st0 + dyoff + a * 8192, &dymap, co0 + 64 * a, pbase, &full[s]);
+                        tc::tma_load_2d(st0 + dyoff + a * C::ATOM_BYTES, &dymap, co0 + 64 * a, pbase, &full[s]);
                 }
             }
         }
@@ -319,7 +321,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                 tc::tc_fence_after();
                 const int nch = min(KB, KT - g * KB);
                 // descriptors built once per stage; a 16-row K step (2048 bytes) adds 128 to the start field
-                const uint64_t ad0 = tc::sw128_desc(tc::smem_u32(base + s * C::STAGE_BYTES), 8192, 1024);
+                const uint64_t ad0 = tc::sw128_desc(tc::smem_u32(base + s * C::STAGE_BYTES), C::ATOM_BYTES, 1024);
 #pragma unroll
                 for (int c = 0; c < KB; c++) {
                     if (c >= nch) break;
@@ -535,11 +537,11 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false, int BKP = 64>
 cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUtensorMap &xmap, dim3 grid,
                       cudaStream_t st) {
-    using C = WgCfg<BN, STAGES, XA, KB>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2>;
+    using C = WgCfg<BN, STAGES, XA, KB, BKP>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2, BKP>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -569,10 +571,10 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
 }
 
 // Whether `splits` CTAs of this configuration can be resident together as one cluster.
-template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false, int BKP = 64>
 bool cluster_fits(int splits) {
-    using C = WgCfg<BN, STAGES, XA, KB>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2>;
+    using C = WgCfg<BN, STAGES, XA, KB, BKP>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2, BKP>;
     static int cached[9] = {-1, -1, -1, -1, -1, -1, -1, -1, -1};
     if (splits < 2 || splits > 8) return false;
     if (cached[splits] < 0) {
@@ -620,6 +622,22 @@ cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, cons
                 case 64: return launch_wg<64, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
                 case 128: return launch_wg<128, 6, false, IM2C, 1>(p, dymap, xmap, grid, st);
                 case 256: return launch_wg<256, 4, false, IM2C, 1>(p, dymap, xmap, grid, st);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+        if (p.wide) {   // 128-pixel chunks, one per stage (each TMA box twice the bytes)
+            if (xa) {
+                switch (bn) {
+                    case 64: return launch_wg<64, 4, true, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
+                    case 128: return launch_wg<128, 3, true, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
+                    case 256: return launch_wg<256, 2, true, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
+                    default: return cudaErrorInvalidValue;
+                }
+            }
+            switch (bn) {
+                case 64: return launch_wg<64, 4, false, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
+                case 128: return launch_wg<128, 3, false, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
+                case 256: return launch_wg<256, 2, false, IM2C, 1, false, 128>(p, dymap, xmap, grid, st);
                 default: return cudaErrorInvalidValue;
             }
         }
@@ -701,8 +719,16 @@ unsigned *tc_wgrad_counters(int n) {
     return r;
 }
 
-bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1, int iss2) {
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1, int iss2, int wide) {
     if (splits < 2 || splits > 8 || !cg_wgrad_cluster_enabled()) return false;
+    if (im2col && wide) {
+        if (xa) return bn == 64    ? cluster_fits<64, 4, true, true, 1, false, 128>(splits)
+                       : bn == 128 ? cluster_fits<128, 3, true, true, 1, false, 128>(splits)
+                                   : bn == 256 && cluster_fits<256, 2, true, true, 1, false, 128>(splits);
+        return bn == 64    ? cluster_fits<64, 4, false, true, 1, false, 128>(splits)
+               : bn == 128 ? cluster_fits<128, 3, false, true, 1, false, 128>(splits)
+                           : bn == 256 && cluster_fits<256, 2, false, true, 1, false, 128>(splits);
+    }
     if (im2col && iss2 && !kb1) {
         if (xa) return bn == 64    ? cluster_fits<64, 2, true, true, 2, true>(splits)
                        : bn == 128 ? cluster_fits<128, 3, true, true, 2, true>(splits)
@@ -733,7 +759,8 @@ bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1, int is
                        : bn == 256 && cluster_fits<256, 4, false, false>(splits);
 }
 
-int tc_wgrad_stages(int bn, int im2col, int kb1) {
+int tc_wgrad_stages(int bn, int im2col, int kb1, int wide) {
+    if (im2col && wide) return bn == 64 ? 4 : (bn == 128 ? 3 : 2);
     if (im2col) return kb1 ? (bn == 128 ? 6 : 4) : (bn == 128 ? 3 : 2);
     return bn == 128 ? 3 : 4;
 }

@@ -29,6 +29,8 @@ struct TcWgradParams {
     // im2col path with two chunks per stage: a second MMA-issuing warp takes the odd chunks into
     // a second accumulator (the epilogue adds the two)
     int iss2;
+    // im2col path: chunks of 128 pixels (p.nchunks / chunks_per_split count them), one per stage
+    int wide;
     // more splits than one cluster holds: `groups` clusters of `csize` splits per tile
     // (cluster dimension z = csize, splits = groups * csize).  Rank r of each cluster writes
     // its row slice of the cluster's sum to gws [tile][group][128][BN]; the last cluster to
@@ -43,9 +45,9 @@ struct TcWgradParams {
 cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                             int mtiles, int ntiles, int splits, cudaStream_t st);
 // Whether splits (2..8) can run as clusters for this tile width / operand side / stage form.
-bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1 = 0, int iss2 = 0);
+bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1 = 0, int iss2 = 0, int wide = 0);
 // Ring stages of the general weight-gradient kernel for a tile width and form.
-int tc_wgrad_stages(int bn, int im2col, int kb1);
+int tc_wgrad_stages(int bn, int im2col, int kb1, int wide = 0);
 // Tile counters of the grouped cluster reduction on the current device: `n` consecutive
 // zero words for one launch (a rotating range of a fixed device array; NULL if unavailable).
 unsigned *tc_wgrad_counters(int n);

@@ -288,6 +288,10 @@ convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int b
  * chunks into a second accumulator, added in the epilogue (another summation order: results
  * stay within the FP32 accumulation bound and bit-reproducible). */
 #define CONVGEMM_WGRAD_TWO_ISSUERS 0x800000
+/* Weight gradient (im2col path): chunks of 128 pixels, one per ring stage, so that every TMA
+ * box carries twice the bytes (the per-box cost, not the bytes, bounds a TMA stream of 8 KB
+ * boxes); the MMAs run in the same order, so dW is bit-identical to the default's. */
+#define CONVGEMM_WGRAD_WIDE_CHUNKS 0x1000000
 #define CONVGEMM_WGRAD_GROUPS(csize) ((csize) == 8 ? 0x300000 : (csize) == 4 ? 0x200000 : (csize) == 2 ? 0x100000 : 0)
 void convgemm_tune_clear(void);
 /* What the tuning table (or the heuristic) selects for the forward, input gradient or weight

@@ -484,6 +484,51 @@ def test_ring_stage_forms_give_identical_results(cglib):
         tc.tune_clear()
 
 
+@pytest.mark.parametrize("b,h,w,c,kn,k,st,pad,bn,splits", [
+    (4, 14, 14, 128, 256, 3, 1, 1, 128, 4),     # X on A, 3x3 im2col boxes, cluster of 4
+    (4, 15, 13, 64, 64, 1, 1, 0, 64, 3),        # 1x1 tiled X boxes, odd pixel count, cluster of 3
+    (2, 28, 28, 256, 128, 3, 2, 1, 256, 9),     # strided, dY on A, reduction kernel (9 splits)
+    (2, 7, 7, 512, 512, 3, 1, 1, 256, 1),       # one split: dW written directly
+])
+def test_wgrad_wide_chunks_bit_identical(cglib, b, h, w, c, kn, k, st, pad, bn, splits):
+    """128-pixel chunks (TMA boxes of twice the bytes, one chunk per stage) issue the MMAs in the
+    same pixel order as two 64-pixel chunks per stage: the same split count gives the same bits."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, st, st)
+    g = C.geom(b, h, w, c, kn, k, k, stride=st, pad=pad)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(17 + c + kn)
+    xd = to_dev_bf16_nhwc(cg, tc, rng.standard_normal(b * h * w * c).astype(np.float32), b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, rng.standard_normal(b * ho * wo * kn).astype(np.float32), b, kn, ho, wo)
+    xa = tc.WGRAD_X_ON_A if kn >= 128 and bn != 64 and k == 3 and st == 1 else 0
+    outs = []
+    try:
+        for flag in (0, tc.WGRAD_WIDE_CHUNKS):
+            tc.tune_set(tc.TUNE_WGRAD, s, bn, splits | xa | flag)
+            plan = tc.wgrad_bf16_plan(s)
+            kern, bnd, stages, cl = tc.tune_describe(tc.TUNE_WGRAD, s)
+            assert kern == 0
+            ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+            d = torch.full((c * k * k * kn,), float("nan"), device="cuda")
+            tc.wgrad_bf16(cg.NHWC, s, dyd, xd, d, ws)
+            outs.append((plan, d))
+        torch.cuda.synchronize()
+        cg.check_device()
+    finally:
+        tc.tune_clear()
+    (p0, d0), (p1, d1) = outs
+    assert torch.isfinite(d1).all()
+    P = b * ho * wo
+    cps64 = -(-(-(-P // 64)) // splits)            # 64-pixel chunks per split
+    cps128 = -(-(-(-P // 128)) // splits)          # 128-pixel chunks per split
+    if cps64 * 64 == cps128 * 128 or (cps64 * 64 >= P and cps128 * 128 >= P):
+        # the same partition of the pixels into splits: the same MMAs in the same order
+        assert torch.equal(d0, d1), (p0, p1)
+    else:
+        assert ((d1 - d0).abs().max() / d0.abs().max()).item() <= 1e-5, (p0, p1)
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc
