@@ -396,10 +396,24 @@ class Net:
             cg.wgrad_f32(cg.NHWC, s, d["dy32"], d["x32"], d["dw32"], self.ws32)
 
 
-def layer_bytes(l, batch, elem=2):
+def layer_bytes(l, batch, op="fwd", elem=2):
+    """Algorithmic HBM bytes of one BF16 operation of a layer: each operand once.
+
+    X counts only the pixels the layer reads: a 1x1 convolution with stride s and no padding
+    reads every s-th pixel of every s-th row, so (ho * wo) pixels, not (h * w).  The input
+    gradient writes all of dX (pixels that no tap reaches are written as zeros), and the
+    weight gradient writes dW in FP32."""
     ho, wo = out_hw(l)
-    return elem * (batch * l["h"] * l["w"] * c8(l["c"]) + batch * ho * wo * l["kn"]) + \
-        elem * l["c"] * l["k"] * l["k"] * l["kn"]
+    cx = c8(l["c"])
+    x_all = batch * l["h"] * l["w"] * cx
+    x_read = batch * ho * wo * cx if (l["k"] == 1 and l["pad"] == 0) else x_all
+    y = batch * ho * wo * l["kn"]
+    w = l["c"] * l["k"] * l["k"] * l["kn"]
+    if op == "fwd":
+        return elem * (x_read + y + w)
+    if op == "dgrad":
+        return elem * (y + w + x_all)
+    return elem * (x_read + y) + 4 * w
 
 
 def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
@@ -416,9 +430,7 @@ def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
         if not d["first"]:
             ops["dgrad"] = lambda: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"])
         fl = conv_flops(l, batch)
-        by = layer_bytes(l, batch)
-        row = {"layer": l["name"], "shape": [l["h"], l["c"], l["kn"], l["k"], l["stride"]], "gflop": fl / 1e9,
-               "mb": by / 1e6, "roofline_us": max(fl / pk_t, by / pk_b) * 1e6}
+        row = {"layer": l["name"], "shape": [l["h"], l["c"], l["kn"], l["k"], l["stride"]], "gflop": fl / 1e9}
         for name, fn in ops.items():
             # `reps` calls captured in one CUDA graph: device time, not host launch cost
             st = torch.cuda.Stream()
@@ -439,8 +451,12 @@ def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
             torch.cuda.synchronize()
             us = a.elapsed_time(b) * 1000 / reps
             del g
+            by = layer_bytes(l, batch, name)
+            roof = max(fl / pk_t, by / pk_b) * 1e6
+            row[name + "_mb"] = by / 1e6
+            row[name + "_roofline_us"] = roof
             row[name + "_us"] = us
-            row[name + "_frac"] = row["roofline_us"] / us
+            row[name + "_frac"] = roof / us
         rows.append(row)
     with open(path, "w") as f:
         json.dump(rows, f, indent=1)
@@ -1232,15 +1248,9 @@ def main():
                "wgrad": "tc_wgrad_kernel + tc_stem_wgrad_kernel + wgrad_reduce_kernel"}
     dominant = max(("fwd", "dgrad", "wgrad"), key=lambda k: fam_summary[k]["ms"])
     dom = fam_summary[dominant]
-    # algorithmic bytes of the family per step: X, dY (or W) read, output written once
-    alg_bytes = 0
-    for d, l in zip(net.L, layers):
-        if dominant == "dgrad" and d["first"]:
-            continue
-        ho, wo = out_hw(l)
-        xb, yb = 2 * batch * l["h"] * l["w"] * c8(l["c"]), 2 * batch * ho * wo * l["kn"]
-        wb = l["c"] * l["k"] * l["k"] * l["kn"]
-        alg_bytes += xb + yb + wb * (4 if dominant == "wgrad" else 2)
+    # algorithmic bytes of the family per step: each operand of each layer once
+    alg_bytes = sum(layer_bytes(l, batch, dominant) for d, l in zip(net.L, layers)
+                    if not (dominant == "dgrad" and d["first"]))
     traffic = profile_traffic(("tc_wgrad_kernel", "tc_stem_wgrad_kernel", "wgrad_reduce_kernel",
                                "wgrad_group_sum_kernel")) \
         if dominant == "wgrad" else None

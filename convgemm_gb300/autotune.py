@@ -30,7 +30,7 @@ from . import tc
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
 OP_CACHE_TAG = "v6"   # op entries: fwd / dgrad with the M-tile, epilogue-warp and ring-stage choices
-WGRAD_CACHE_TAG = "v10"   # wgrad: ring stages, two issuers, 128-pixel chunks, direct single-split writes, 2..8-split clusters, grouped clusters, slab kernel
+WGRAD_CACHE_TAG = "v11"   # wgrad: ring stages, two issuers, 128-pixel chunks, TMA-written single-split and one-cluster dW, grouped clusters, slab kernel
 
 
 def cache_path() -> str:

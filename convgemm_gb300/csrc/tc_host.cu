@@ -61,6 +61,12 @@ EncodeIm2colFn encode_im2col_fn() {
 convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, const unsigned long long *dims,
                                   const unsigned long long *strides_bytes, const unsigned *box, const unsigned *estr,
                                   int swizzle128) {
+    return tc_make_map_nd_dt(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, ptr, dims, strides_bytes, box, estr, swizzle128);
+}
+
+convgemm_status_t tc_make_map_nd_dt(CUtensorMap *map, CUtensorMapDataType dt, int rank, const void *ptr,
+                                     const unsigned long long *dims, const unsigned long long *strides_bytes,
+                                     const unsigned *box, const unsigned *estr, int swizzle128) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     if ((uintptr_t) ptr & 15) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA operand not 16-byte aligned");
@@ -75,7 +81,7 @@ convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, co
             if (st[i] % 16) return cg_set_error(CONVGEMM_ERROR_INVALID_VALUE, "TMA stride not a multiple of 16 bytes");
         }
     }
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t) rank, const_cast<void *>(ptr), d, st, b, e,
+    CUresult r = fn(map, dt, (cuuint32_t) rank, const_cast<void *>(ptr), d, st, b, e,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int) r);
@@ -652,6 +658,11 @@ bool wgrad_im2col_ok(const cg_shape &s, const ConvGeom &g) {
            up_w >= -128 && up_w <= 127 && s.vstride <= 8 && s.hstride <= 8;
 }
 
+// Workspace of the one-cluster exchange of partial tiles: [tile][split][128 x bn] FP32.
+size_t wgrad_xchg_bytes(const WgPlan &w) {
+    return sizeof(float) * 128 * (size_t) w.bn * (size_t) w.mtiles * (size_t) w.ntiles * (size_t) w.splits;
+}
+
 WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     const cg_shape s = cg_from_public(ps);
     const ConvGeom g = make_geom(s);
@@ -717,6 +728,8 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.ws_bytes = sizeof(float) * (size_t) (w.splits + tc_wgrad_groups(w.splits)) * (size_t) w.Nx * (size_t) s.kn;
     w.csize = w.groups = 0;
     if (w.slab) return w;
+    // 2..8 splits as one cluster exchange whole 128 x bn partial tiles through the workspace
+    if (!w.stem && w.splits >= 2 && w.splits <= 8 && wgrad_xchg_bytes(w) > w.ws_bytes) w.ws_bytes = wgrad_xchg_bytes(w);
     // more splits than one cluster: clusters of up to 8 splits, reduced in the kernel (the
     // workspace is sized for the smallest cluster, so that it does not depend on the device)
     w.csize = w.groups = 0;
@@ -843,6 +856,32 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
         if (!p.counters) return cg_set_error(CONVGEMM_ERROR_CUDA, "convgemm_wgrad_bf16: tile counters unavailable");
     } else {
         p.cluster = tc_wgrad_cluster_ok(w.bn, w.xa, p.im2col, w.splits, w.kb1, w.iss2, w.wide);
+    }
+    if ((p.direct || (p.cluster && p.groups <= 1)) && layout == CONVGEMM_NHWC && s.kn % 4 == 0 && w.Cp % 32 == 0 &&
+        !((uintptr_t) dw & 15)) {
+        // the kernel writes dW itself: [ci][tap][co] as (co, tap, ci), 32 x 1 x 32 FP32 boxes
+        // (rows of 128 bytes, swizzled)
+        const unsigned long long dims[3] = {(unsigned long long) s.kn, (unsigned long long) (s.kh * s.kw),
+                                            (unsigned long long) s.c};
+        const unsigned long long str[2] = {(unsigned long long) s.kn * 4, (unsigned long long) s.kn * s.kh * s.kw * 4};
+        const unsigned box[3] = {32, 1, 32}, estr[3] = {1, 1, 1};
+        if (convgemm_status_t e = tc_make_map_nd_dt(&p.dwmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, dw, dims, str, box, estr, 1))
+            return e;
+        p.dw_tma = 1;
+        p.xchg = p.cluster && p.groups <= 1 && !((uintptr_t) workspace & 15) &&
+                 workspace_bytes >= wgrad_xchg_bytes(w);
+    }
+    const int Mext = w.xa ? w.Nx : s.kn, Next = w.xa ? s.kn : w.Nx;
+    if (!p.direct && !p.cluster && Next % 4 == 0 && !((uintptr_t) workspace & 15)) {
+        // split partials [split][Mext][Next] written by TMA, clipped per split
+        const unsigned long long dims[3] = {(unsigned long long) Next, (unsigned long long) Mext,
+                                            (unsigned long long) w.splits};
+        const unsigned long long str[2] = {(unsigned long long) Next * 4, (unsigned long long) Next * Mext * 4};
+        const unsigned box[3] = {32, 32, 1}, estr[3] = {1, 1, 1};
+        if (convgemm_status_t e =
+                tc_make_map_nd_dt(&p.wsmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, workspace, dims, str, box, estr, 1))
+            return e;
+        p.ws_tma = 1;
     }
     if (convgemm_status_t e = cg_cuda_check(
             tc_wgrad_launch(p, map, xmap, w.bn, w.xa, w.mtiles, w.ntiles, w.splits, st), "weight-gradient launch"))

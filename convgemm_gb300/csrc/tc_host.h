@@ -31,6 +31,10 @@ bool tc_plan_im2col(TcPlan &pl);
 convgemm_status_t tc_make_map_nd(CUtensorMap *map, int rank, const void *ptr, const unsigned long long *dims,
                                   const unsigned long long *strides_bytes, const unsigned *box, const unsigned *estr,
                                   int swizzle128);
+// The same for another element type.
+convgemm_status_t tc_make_map_nd_dt(CUtensorMap *map, CUtensorMapDataType dt, int rank, const void *ptr,
+                                     const unsigned long long *dims, const unsigned long long *strides_bytes,
+                                     const unsigned *box, const unsigned *estr, int swizzle128);
 // Stride-1 convolutions with 64-channel input blocks and 2..16 taps, operands read from
 // input slabs (tc_slab.cu): the forward or input-gradient plan decides.
 bool tc_slab_applicable(const TcPlan &pl);

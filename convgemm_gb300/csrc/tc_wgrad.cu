@@ -32,6 +32,57 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
+// FP32 TMA store of one 32 x 1 x 32 box of dW, coordinates (co, tap, ci).
+__device__ __forceinline__ void wg_store_3d(const CUtensorMap *map, uint32_t src, int co, int tap, int ci) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"((uint64_t) map),
+                 "r"(src), "r"(co), "r"(tap), "r"(ci)
+                 : "memory");
+}
+__device__ __forceinline__ void wg_bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void wg_bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void wg_bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) shared -> global.
+__device__ __forceinline__ void wg_bulk_store(void *dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes) : "memory");
+}
+// FP32 TMA store of one 32 x 32 x 1 box of the split partials (n, m, split).
+__device__ __forceinline__ void wg_store_part(const CUtensorMap *map, uint32_t src, int n, int m, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"((uint64_t) map),
+                 "r"(src), "r"(n), "r"(m), "r"(z)
+                 : "memory");
+}
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) global -> shared.
+__device__ __forceinline__ void wg_bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(tc::smem_u32(bar))
+                 : "memory");
+}
+
+// One 32 x 32 FP32 block into a 4 KB staging buffer laid out as a dW box: 32 rows (K indices
+// n = tap*Cp + ci) of 32 output channels, 16-byte chunk q of row r at chunk q ^ (r & 7) (the
+// 128-byte swizzle of the store's tensor map; conflict-free shared-memory stores).  The thread
+// holds row `lane` of the block, v[j] = column j.  With X on the A side the block's rows are K
+// indices; otherwise they are output channels and the block is transposed on the way in.
+template <bool XA>
+__device__ __forceinline__ void wg_stage_block(uint32_t buf, int lane, const uint32_t (&v)[32]) {
+    if constexpr (XA) {
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(buf + lane * 128 + ((q ^ (lane & 7)) << 4)),
+                         "r"(v[4 * q]), "r"(v[4 * q + 1]), "r"(v[4 * q + 2]), "r"(v[4 * q + 3])
+                         : "memory");
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; j++)
+            asm volatile("st.shared.b32 [%0], %1;" ::"r"(buf + j * 128 + (((lane >> 2) ^ (j & 7)) << 4) + ((lane & 3) << 2)),
+                         "r"(v[j])
+                         : "memory");
+    }
+}
+
 // KB chunks of BK pixels per pipeline stage: one full barrier and one MMA commit
 // cover KB chunks (the barrier round trip, not the loads or the MMAs, bounds a
 // one-chunk stage).
@@ -78,6 +129,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     uint64_t *empty = full + STAGES;
     uint64_t *accum = empty + STAGES;
     uint32_t *tmem_holder = (uint32_t *) (accum + 1);
+    uint64_t *xbar = accum + 2;   // four: the epilogue warps' copies of the exchanged blocks
 
     constexpr int GW = WgWarps<IM2C>::GW;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -87,6 +139,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
             tc::mbar_init(&empty[s], NISS);
         }
         tc::mbar_init(accum, NISS);
+        for (int i = 0; i < 4; i++) tc::mbar_init(&xbar[i], 1);
         tc::fence_mbar_init();
         tc::prefetch_tmap(&dymap);
         if (IM2C) tc::prefetch_tmap(&xmap);
@@ -110,6 +163,65 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     const int KT = min(p.chunks_per_split, p.nchunks - chunk0);   // chunks of this split
     const int NG = (KT + KB - 1) / KB;                              // pipeline stages they fill
     bool ok = true;
+    // 32 accumulator columns of this warp's rows: the accumulator, plus the second issuer's (odd chunks)
+    auto ld_acc = [&](int c0, uint32_t(&v)[32]) {
+        tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
+        tc::tmem_ld_wait();
+        if constexpr (ISS2) {
+            if (KT >= 2) {
+                uint32_t u[32];
+                tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) (BN + c0), u);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int i = 0; i < 32; i++) v[i] = __float_as_uint(__fadd_rn(__uint_as_float(v[i]), __uint_as_float(u[i])));
+            }
+        }
+    };
+    // fn(c0, v) for the 32-column blocks c0 = 0, 32, ... of this warp's accumulator rows, with the
+    // next block's TMEM load in flight while fn runs (each use of v follows its wait)
+    auto for_acc_blocks = [&](auto &&fn) {
+        uint32_t va[32], ua[32], vb[32], ub[32];
+        const uint32_t rowb = tmem + ((uint32_t) (warp * 32) << 16);
+        auto issue = [&](int c0, uint32_t(&v)[32], uint32_t(&u)[32]) {
+            tc::tmem_ld_32x32b_x32(rowb + (uint32_t) c0, v);
+            if constexpr (ISS2) {
+                if (KT >= 2) tc::tmem_ld_32x32b_x32(rowb + (uint32_t) (BN + c0), u);
+            }
+        };
+        auto finish = [&](uint32_t(&v)[32], const uint32_t(&u)[32]) {
+            if constexpr (ISS2) {
+                if (KT >= 2) {
+#pragma unroll
+                    for (int i = 0; i < 32; i++) v[i] = __float_as_uint(__fadd_rn(__uint_as_float(v[i]), __uint_as_float(u[i])));
+                }
+            }
+        };
+        issue(0, va, ua);
+        tc::tmem_ld_wait();
+        finish(va, ua);
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 64) {
+            const bool has_b = c0 + 32 < BN, has_a = c0 + 64 < BN;
+            if (has_b) issue(c0 + 32, vb, ub);
+            fn(c0, va);
+            if (!has_b) break;
+            tc::tmem_ld_wait();
+            finish(vb, ub);
+            if (has_a) issue(c0 + 64, va, ua);
+            fn(c0 + 32, vb);
+            if (has_a) {
+                tc::tmem_ld_wait();
+                finish(va, ua);
+            }
+        }
+    };
+    // One cluster (2..8 splits) writing dW by TMA: the ranks exchange their partial tiles' 32 x 32
+    // blocks through the workspace; each block's owner copies the ranks' copies into its idle ring
+    // ([blocks per rank][ranks] 4 KB slots, then 8 KB of staging per epilogue warp) and adds them.
+    constexpr int NBLK = 4 * (BN / 32);
+    constexpr uint32_t RECV_MAX = (uint32_t) (NBLK + 7) * 4096u;
+    constexpr bool PUSH_FITS = (size_t) STAGES * C::STAGE_BYTES >= (size_t) RECV_MAX + 4 * 8192;
+    const bool push = PUSH_FITS && p.cluster && p.xchg;
 
     if (IM2C && warp < 4) {
         // one thread: im2col TMA for each 64-channel X atom (a fixed tap and channel chunk
@@ -227,25 +339,14 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     if (warp < 4) {
         // epilogue: FP32 partial tile -> workspace [split][Mext][Next]
         if (ok) ok = tc::mbar_wait(accum, 0, p.err, 13);
+        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
         tc::tc_fence_after();
-        // 32 columns of this warp's rows: the accumulator, plus the second issuer's (odd chunks)
-        auto ld_acc = [&](int c0, uint32_t(&v)[32]) {
-            tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) c0, v);
-            tc::tmem_ld_wait();
-            if constexpr (ISS2) {
-                if (KT >= 2) {
-                    uint32_t u[32];
-                    tc::tmem_ld_32x32b_x32(tmem + ((uint32_t) (warp * 32) << 16) + (uint32_t) (BN + c0), u);
-                    tc::tmem_ld_wait();
-#pragma unroll
-                    for (int i = 0; i < 32; i++) v[i] = __float_as_uint(__fadd_rn(__uint_as_float(v[i]), __uint_as_float(u[i])));
-                }
-            }
-        };
         const int m = mrow0 + warp * 32 + lane;
         const int Mext = XA ? p.Nx : p.kn, Next = XA ? p.kn : p.Nx;
         float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
-        if (p.cluster) {
+        if (push) {
+            // the partial tile leaves TMEM after the cluster barrier below
+        } else if (p.cluster) {
             // this split's partial tile into shared memory (the ring is idle now), rows padded by
             // 4 floats against bank conflicts; the cluster adds the splits below
             float *R = reinterpret_cast<float *>(base);
@@ -264,6 +365,31 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                     dst[q] = make_float4(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1]),
                                          __uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3]));
             }
+        } else if (ok && p.direct && p.dw_tma) {
+            // single split: 32 x 32 blocks staged in the idle ring (two 4 KB buffers per warp) and
+            // written by TMA, one store per block (a block lies in one tap: Cp % 32 == 0)
+            const uint32_t stg = tc::smem_u32(base) + (uint32_t) warp * 8192u;
+            for_acc_blocks([&](int c0, const uint32_t(&v)[32]) {
+                const uint32_t buf = stg + (uint32_t) ((c0 >> 5) & 1) * 4096u;
+                if (c0 >= 64) {   // the store issued from this buffer two blocks ago has read it
+                    if (lane == 0) wg_bulk_wait_read<1>();
+                    __syncwarp();
+                }
+                wg_stage_block<XA>(buf, lane, v);
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    const int nf = XA ? mrow0 + warp * 32 : ncol0 + c0;   // first K index of the block
+                    const int cf = XA ? ncol0 + c0 : mrow0 + warp * 32;   // first output channel
+                    uint32_t tap = 0, ci = 0;
+                    if (nf < p.Nx) p.dcp.divmod((uint32_t) nf, tap, ci);
+                    if (nf < p.Nx && cf < p.kn && (int) ci < p.C)
+                        wg_store_3d(&p.dwmap, buf, cf, (int) tap, (int) ci);   // rows ci >= C, co >= kn clipped
+                    wg_bulk_commit();
+                }
+            });
+            if (lane == 0) wg_bulk_wait_all();
+            __syncwarp();
         } else if (ok && p.direct) {
             // single split: dW written in the reference layout (lanes hold consecutive rows)
             const int khw = p.kh * p.kw;
@@ -285,6 +411,27 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                     p.dw[o] = __uint_as_float(v[jj]);
                 }
             }
+        } else if (ok && p.ws_tma) {
+            // partial tile -> workspace [split][Mext][Next]: 32 x 32 blocks staged (rows = this
+            // warp's accumulator rows) and written by TMA, clipped at Mext and Next
+            const uint32_t stg = tc::smem_u32(base) + (uint32_t) warp * 8192u;
+            const int mb = mrow0 + warp * 32;
+            for_acc_blocks([&](int c0, const uint32_t(&v)[32]) {
+                const uint32_t buf = stg + (uint32_t) ((c0 >> 5) & 1) * 4096u;
+                if (c0 >= 64) {
+                    if (lane == 0) wg_bulk_wait_read<1>();
+                    __syncwarp();
+                }
+                wg_stage_block<true>(buf, lane, v);
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    if (mb < Mext && ncol0 + c0 < Next) wg_store_part(&p.wsmap, buf, ncol0 + c0, mb, (int) blockIdx.z);
+                    wg_bulk_commit();
+                }
+            });
+            if (lane == 0) wg_bulk_wait_all();
+            __syncwarp();
         } else if (ok) {
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -338,7 +485,117 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
         __syncwarp();
     }
 
-    if (p.cluster) {
+    if (push) {
+        // partial tiles exchanged through L2: each rank writes its 32 x 32 blocks to the workspace
+        // ([tile][rank][block][32 x 32], 16-byte chunks of row r at chunk q ^ (r & 7)) by bulk
+        // copies, the cluster barrier publishes them, and each block's owner (rank b % nrank)
+        // copies the ranks' copies of its blocks into its idle ring, adds them in rank order and
+        // writes dW by TMA
+        uint32_t rank, nrank;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+        asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(nrank));
+        const int tile = blockIdx.x + gridDim.x * blockIdx.y;
+        float *gp = p.ws + (size_t) tile * nrank * NBLK * 1024;
+        if (warp < 4) {
+            // each block staged in shared memory (rows = this warp's accumulator rows) and written
+            // as one 4 KB bulk copy
+            const uint32_t stg = tc::smem_u32(base) + RECV_MAX + (uint32_t) warp * 8192u;
+            auto send = [&](int c0, const uint32_t(&v)[32]) {
+                const int cb = c0 >> 5;
+                const uint32_t buf = stg + (uint32_t) (cb & 1) * 4096u;
+                if (cb >= 2) {
+                    if (lane == 0) wg_bulk_wait_read<1>();
+                    __syncwarp();
+                }
+                wg_stage_block<true>(buf, lane, v);
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    wg_bulk_store(gp + ((size_t) rank * NBLK + cb * 4 + warp) * 1024, buf, 4096u);
+                    wg_bulk_commit();
+                }
+            };
+            if (ok && KT > 0) {
+                for_acc_blocks(send);
+            } else {   // a timed-out split adds zero
+                uint32_t z[32];
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) z[jj] = 0u;
+#pragma unroll 1
+                for (int c0 = 0; c0 < BN; c0 += 32) send(c0, z);
+            }
+            if (lane == 0) wg_bulk_wait_all();   // written before the barrier publishes them
+            __syncwarp();
+            asm volatile("fence.proxy.async;" ::: "memory");
+        }
+        asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+        if (warp < 4) {
+            asm volatile("fence.proxy.async;" ::: "memory");
+            const uint32_t Rloc = tc::smem_u32(base);
+            const int per = (NBLK + (int) nrank - 1) / (int) nrank;   // blocks each rank owns (at most)
+            int nb = 0;
+            for (int j = warp; j < per; j += 4)
+                if (j * (int) nrank + (int) rank < NBLK) nb++;
+            if (lane == 0 && nb > 0) {
+                tc::mbar_arrive_expect_tx(&xbar[warp], (uint32_t) (nb * (int) nrank) * 4096u);
+                for (int j = warp; j < per; j += 4) {
+                    const int b = j * (int) nrank + (int) rank;
+                    if (b >= NBLK) break;
+                    for (int z = 0; z < (int) nrank; z++)
+                        wg_bulk_load(Rloc + (uint32_t) (j * (int) nrank + z) * 4096u, gp + ((size_t) z * NBLK + b) * 1024,
+                                     4096u, &xbar[warp]);
+                }
+            }
+            const bool okx = nb == 0 || tc::mbar_wait(&xbar[warp], 0, p.err, 14);
+            const uint32_t stg = Rloc + RECV_MAX + (uint32_t) warp * 8192u;
+            int i = 0;
+#pragma unroll 1
+            for (int j = warp; okx && j < per; j += 4, i++) {
+                const int b = j * (int) nrank + (int) rank;
+                if (b >= NBLK) break;
+                const int rb = b & 3, cb = b >> 2;
+                float a[32];
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) a[jj] = 0.0f;
+#pragma unroll 1
+                for (int z = 0; z < (int) nrank; z++) {
+                    const uint32_t src = Rloc + (uint32_t) (j * (int) nrank + z) * 4096u + (uint32_t) lane * 128u;
+#pragma unroll
+                    for (int q = 0; q < 8; q++) {
+                        float4 t;
+                        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                     : "=f"(t.x), "=f"(t.y), "=f"(t.z), "=f"(t.w)
+                                     : "r"(src + ((q ^ (lane & 7)) << 4)));
+                        a[4 * q] = __fadd_rn(a[4 * q], t.x);
+                        a[4 * q + 1] = __fadd_rn(a[4 * q + 1], t.y);
+                        a[4 * q + 2] = __fadd_rn(a[4 * q + 2], t.z);
+                        a[4 * q + 3] = __fadd_rn(a[4 * q + 3], t.w);
+                    }
+                }
+                uint32_t v[32];
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) v[jj] = __float_as_uint(a[jj]);
+                const uint32_t buf = stg + (uint32_t) (i & 1) * 4096u;
+                if (i >= 2) {
+                    if (lane == 0) wg_bulk_wait_read<1>();
+                    __syncwarp();
+                }
+                wg_stage_block<XA>(buf, lane, v);
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) {
+                    const int nf = XA ? mrow0 + rb * 32 : ncol0 + cb * 32;
+                    const int cf = XA ? ncol0 + cb * 32 : mrow0 + rb * 32;
+                    uint32_t tap = 0, ci = 0;
+                    if (nf < p.Nx) p.dcp.divmod((uint32_t) nf, tap, ci);
+                    if (nf < p.Nx && cf < p.kn && (int) ci < p.C) wg_store_3d(&p.dwmap, buf, cf, (int) tap, (int) ci);
+                    wg_bulk_commit();
+                }
+            }
+            if (lane == 0) wg_bulk_wait_all();
+            __syncwarp();
+        }
+    } else if (p.cluster) {
         // dW = sum of the cluster's partial tiles in split (cluster rank) order; rank r adds rows
         // [r*rows, (r+1)*rows) across all ranks' shared memory and writes them.  With grouped
         // clusters (p.groups > 1) the slice goes to gws instead, and the last cluster of the

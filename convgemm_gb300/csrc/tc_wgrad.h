@@ -39,6 +39,18 @@ struct TcWgradParams {
     int groups, csize;
     float *gws;
     unsigned *counters;       // mtiles * ntiles * csize words, zero between calls
+    // dW of the NHWC API ([ci][kh][kw][co], kn % 4 == 0, Cp % 32 == 0) as a 3-D FP32 tensor
+    // (co, tap, ci) with 32 x 1 x 32 boxes and 128-byte swizzle: the single-split epilogue and
+    // the one-cluster reduction stage 32 x 32 blocks in shared memory and write them by TMA
+    int dw_tma;
+    // with dw_tma and one cluster: the splits' partial tiles meet in ws ([tile][rank][32 x 32
+    // blocks], 16-byte aligned) instead of distributed shared memory
+    int xchg;
+    CUtensorMap dwmap;
+    // several splits, no cluster: the partial tiles go to ws by TMA, ws viewed as the FP32 tensor
+    // (n, m, split) of extents (Next, Mext, splits), 32 x 32 x 1 boxes, 128-byte swizzle
+    int ws_tma;
+    CUtensorMap wsmap;
 };
 
 // xmap: im2col map of x (64 pixels x 64 channels per load), used when p.im2col.

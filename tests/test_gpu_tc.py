@@ -529,6 +529,49 @@ def test_wgrad_wide_chunks_bit_identical(cglib, b, h, w, c, kn, k, st, pad, bn, 
         assert ((d1 - d0).abs().max() / d0.abs().max()).item() <= 1e-5, (p0, p1)
 
 
+@pytest.mark.parametrize("b,h,w,c,kn,k,st,pad,bn,aux", [
+    (2, 7, 7, 512, 512, 3, 1, 1, 128, 1),             # one split, dY on A: blocks transposed into the boxes
+    (2, 7, 7, 512, 512, 3, 1, 1, 128, 1 | 0x1000000),  # the same with 128-pixel chunks
+    (2, 7, 7, 512, 512, 3, 1, 1, 256, 1 | 0x10000),    # one split, X on A
+    (4, 14, 14, 256, 256, 3, 1, 1, 128, 4),           # cluster of 4: blocks pushed to their owners
+    (4, 14, 14, 128, 256, 3, 1, 1, 128, 3 | 0x10000),  # cluster of 3, X on A (uneven block ownership)
+    (16, 7, 7, 2048, 512, 1, 1, 0, 256, 8),           # 13 chunks: cluster of 7, 256-wide tiles
+    (4, 14, 14, 128, 100, 3, 1, 1, 0, 2),             # kn = 100: the last channel block clipped
+    (2, 11, 11, 30, 100, 3, 1, 1, 0, 1),              # 30 channels padded to 32: rows past C clipped
+])
+def test_wgrad_tma_epilogue_matches_scalar_layout(cglib, b, h, w, c, kn, k, st, pad, bn, aux):
+    """dW of the NHWC API is staged in 32 x 32 blocks and written by TMA (one split, or one
+    cluster of 2-8 splits whose blocks meet at their owner rank); the NCHW API writes the same
+    sums element by element.  The two must hold the same bits."""
+    from convgemm_gb300 import tc
+    cg = cglib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, st, st)
+    g = C.geom(b, h, w, c, kn, k, k, stride=st, pad=pad)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(23 + c + kn + bn)
+    xd = to_dev_bf16_nhwc(cg, tc, rng.standard_normal(b * h * w * c).astype(np.float32), b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, rng.standard_normal(b * ho * wo * kn).astype(np.float32), b, kn, ho, wo)
+    try:
+        tc.tune_set(tc.TUNE_WGRAD, s, bn, aux)
+        kern, _, _, cl = tc.tune_describe(tc.TUNE_WGRAD, s)
+        sp = tc.wgrad_bf16_plan(s)[1]
+        assert kern == 0 and sp <= (aux & 0xffff) and cl == (sp if sp <= 8 else 1), (kern, sp, cl)
+        ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+        out = {}
+        for layout in (cg.NHWC, cg.NCHW):
+            d = torch.full((c * k * k * kn,), float("nan"), device="cuda")
+            tc.wgrad_bf16(layout, s, dyd, xd, d, ws)
+            out[layout] = d
+        torch.cuda.synchronize()
+        cg.check_device()
+    finally:
+        tc.tune_clear()
+    nhwc = out[cg.NHWC].view(c, k * k, kn).permute(2, 0, 1).contiguous()
+    nchw = out[cg.NCHW].view(kn, c, k * k)
+    assert torch.isfinite(nhwc).all()
+    assert torch.equal(nhwc, nchw)
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc
