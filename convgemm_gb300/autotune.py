@@ -30,7 +30,7 @@ from . import tc
 WIDTHS = (64, 128, 256)
 CACHE_VERSION = "group-bn-v1"
 OP_CACHE_TAG = "v6"   # op entries: fwd / dgrad with the M-tile, epilogue-warp and ring-stage choices
-WGRAD_CACHE_TAG = "v11"   # wgrad: ring stages, two issuers, 128-pixel chunks, TMA-written single-split and one-cluster dW, grouped clusters, slab kernel
+WGRAD_CACHE_TAG = "v12"   # wgrad: ring stages, two issuers, 128-pixel chunks, TMA-written single-split and one-cluster dW, grouped clusters, CTA pairs, slab kernel
 
 
 def cache_path() -> str:
@@ -225,6 +225,14 @@ def op_candidates(op: int, s):
     out += [(w, sp | tc.WGRAD_GROUPS(cs)) for w, sp in list(out)
             if (sp & 0xffff) > 8 and not sp & (tc.WGRAD_STAGES1 | tc.WGRAD_TWO_ISSUERS | tc.WGRAD_WIDE_CHUNKS)
             for cs in (2, 4, 8)]
+    # CTA pairs (256 x 256 tiles), both operand sides, around their own split heuristic
+    if tc.c8(s.c) % 64 == 0:
+        for xa in (0, tc.WGRAD_X_ON_A) if s.kn >= 128 else (0,):
+            for w in (128, 256):
+                tc.tune_set(op, s, w, tc.WGRAD_PAIR | xa)
+                _, s4, _ = tc.wgrad_bf16_plan(s)
+                out += [(w, sp | tc.WGRAD_PAIR | xa) for sp in sorted({max(1, s4 // 2), s4, min(mx, 2 * s4)})]
+        tc.tune_set(op, s, 0, 0)
     # stride-1 layers with 128-channel blocks: the slab kernel around its own split heuristic
     tc.tune_set(op, s, 0, tc.WGRAD_SLAB)
     bn_s, s3, _ = tc.wgrad_bf16_plan(s)

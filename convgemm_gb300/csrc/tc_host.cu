@@ -646,6 +646,7 @@ struct WgPlan {
     int kb1;             // im2col path: one chunk per ring stage (twice the stages)
     int iss2;            // im2col path, two chunks per stage: two MMA-issuing warps
     int wide;            // im2col path: 128-pixel chunks (twice the bytes per TMA box), one per stage
+    int pair;            // im2col path: CTA pairs, 256 x bn tiles (bn 128 / 256, mtiles even, wide chunks)
     int bk;              // pixels per chunk (64, or 128 when wide)
     size_t ws_bytes;
 };
@@ -674,7 +675,8 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.Nx = s.kh * s.kw * w.Cp;
     const bool im2col = wgrad_im2col_ok(s, g);
     const int aux_splits = t.splits & 0xffff;
-    w.wide = im2col && (t.splits & CONVGEMM_WGRAD_WIDE_CHUNKS) ? 1 : 0;
+    w.pair = im2col && (t.splits & CONVGEMM_WGRAD_PAIR) ? 1 : 0;
+    w.wide = im2col && (w.pair || (t.splits & CONVGEMM_WGRAD_WIDE_CHUNKS)) ? 1 : 0;
     w.kb1 = im2col && !w.wide && (t.splits & CONVGEMM_WGRAD_STAGES1) ? 1 : 0;
     w.iss2 = im2col && !w.kb1 && !w.wide && (t.splits & CONVGEMM_WGRAD_TWO_ISSUERS) ? 1 : 0;
     w.bk = w.wide ? 128 : 64;
@@ -696,7 +698,9 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
         w.bn = w.Nx >= 256 ? 256 : (w.Nx > 64 ? 128 : 64);
         if (t.bn) w.bn = t.bn;
     }
+    if (w.pair) w.bn = t.bn == 128 ? 128 : 256;   // pair tiles: 256 x 128 or 256 x 256
     w.mtiles = (Mext + 127) / 128;
+    if (w.pair) w.mtiles += w.mtiles & 1;   // the two CTAs of a pair take adjacent M tiles
     w.ntiles = (Next + w.bn - 1) / w.bn;
     w.nchunks = (int) ((g.P + w.bk - 1) / w.bk);
     const int base = w.mtiles * w.ntiles;
@@ -729,11 +733,12 @@ WgPlan plan_wgrad(const convgemm_shape_t &ps) {
     w.csize = w.groups = 0;
     if (w.slab) return w;
     // 2..8 splits as one cluster exchange whole 128 x bn partial tiles through the workspace
-    if (!w.stem && w.splits >= 2 && w.splits <= 8 && wgrad_xchg_bytes(w) > w.ws_bytes) w.ws_bytes = wgrad_xchg_bytes(w);
+    if (!w.stem && !w.pair && w.splits >= 2 && w.splits <= 8 && wgrad_xchg_bytes(w) > w.ws_bytes)
+        w.ws_bytes = wgrad_xchg_bytes(w);
     // more splits than one cluster: clusters of up to 8 splits, reduced in the kernel (the
     // workspace is sized for the smallest cluster, so that it does not depend on the device)
     w.csize = w.groups = 0;
-    if (!w.stem && w.splits > 8) {
+    if (!w.stem && !w.pair && w.splits > 8) {
         const size_t tile_bytes = sizeof(float) * 128 * (size_t) w.bn * (size_t) w.mtiles * (size_t) w.ntiles;
         const size_t grouped = tile_bytes * (size_t) ((w.splits + 1) / 2);
         if (grouped > w.ws_bytes) w.ws_bytes = grouped;
@@ -846,7 +851,10 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
     p.kb1 = w.kb1;
     p.iss2 = w.iss2;
     p.wide = w.wide;
-    if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
+    p.pair = w.pair;
+    if (w.pair) {
+        p.cluster = 0;   // the cluster is the pair; several splits reduce through the workspace
+    } else if (w.groups > 1 && !((uintptr_t) workspace & 15)) {
         // clusters of csize splits; the tile's last cluster adds the clusters' sums
         p.cluster = 1;
         p.groups = w.groups;
@@ -917,8 +925,9 @@ extern "C" convgemm_status_t convgemm_tune_describe(int op, const convgemm_shape
         }
         const ConvGeom g = make_geom(s);
         const int im2col = wgrad_im2col_ok(s, g);
-        *stages = tc_wgrad_stages(w.bn, im2col, w.kb1, w.wide);
-        if (w.groups > 1) *cluster = w.csize;
+        *stages = tc_wgrad_stages(w.bn, im2col, w.kb1, w.wide, w.pair);
+        if (w.pair) *cluster = 2;
+        else if (w.groups > 1) *cluster = w.csize;
         else if (tc_wgrad_cluster_ok(w.bn, w.xa, im2col, w.splits, w.kb1, w.iss2, w.wide)) *cluster = w.splits;
         return CONVGEMM_SUCCESS;
     }

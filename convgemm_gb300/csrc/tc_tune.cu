@@ -37,7 +37,7 @@ extern "C" convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *s
     const bool mt_op = op == CONVGEMM_TUNE_FWD || op == CONVGEMM_TUNE_DGRAD;
     // forward / input gradient: M tiles per weight tile (1 / 2) + 4 for eight epilogue warps
     // weight gradient: pixel splits in bits 0-15, CONVGEMM_WGRAD_* flags above
-    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? (splits >= 0 && (splits & ~0x1fbffff) == 0)
+    const bool aux_ok = op == CONVGEMM_TUNE_WGRAD ? (splits >= 0 && (splits & ~0x3fbffff) == 0)
                         : mt_op ? ((splits & ~24) == 0 || (splits & ~24) == 1 || (splits & ~24) == 2 ||
                                    (splits & ~24) == 5 || (splits & ~24) == 6)
                                 : splits == 0;

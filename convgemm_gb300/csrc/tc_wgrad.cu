@@ -86,16 +86,19 @@ __device__ __forceinline__ void wg_stage_block(uint32_t buf, int lane, const uin
 // KB chunks of BK pixels per pipeline stage: one full barrier and one MMA commit
 // cover KB chunks (the barrier round trip, not the loads or the MMAs, bounds a
 // one-chunk stage).
-template <int BN, int STAGES, bool XA, int KB = 1, int BKP = 64>
+// PAIR: a CTA pair shares 256 x BN tiles (cta_group::2 MMAs): each CTA holds its 128 A rows and
+// half of the BN B columns.
+template <int BN, int STAGES, bool XA, int KB = 1, int BKP = 64, bool PAIR = false>
 struct WgCfg {
     static constexpr int BM = 128, BK = BKP;  // BK pixels per chunk (64, or 128: each TMA box twice as large)
+    static constexpr int BNL = PAIR ? BN / 2 : BN;   // B columns in this CTA's shared memory
     static constexpr uint32_t ATOM_BYTES = (uint32_t) BK * 128;   // 64 channels x BK pixels
     static constexpr uint32_t A_BYTES = BM * BK * 2;
-    static constexpr uint32_t B_BYTES = BN * BK * 2;
+    static constexpr uint32_t B_BYTES = BNL * BK * 2;
     static constexpr uint32_t CHUNK_BYTES = A_BYTES + B_BYTES;
     static constexpr uint32_t STAGE_BYTES = KB * CHUNK_BYTES;
-    static constexpr int X_ATOMS = (XA ? BM : BN) / 64;    // 64-channel atoms gathered from X
-    static constexpr int DY_ATOMS = (XA ? BN : BM) / 64;   // 64-channel atoms loaded from dY
+    static constexpr int X_ATOMS = (XA ? BM : BNL) / 64;    // 64-channel atoms gathered from X
+    static constexpr int DY_ATOMS = (XA ? BNL : BM) / 64;   // 64-channel atoms loaded from dY
     static constexpr uint32_t DY_BYTES = DY_ATOMS * ATOM_BYTES;
     static constexpr int LAG = STAGES / 2;  // half the ring in flight, half queued for the MMA
     static constexpr size_t SMEM = 1024 + (size_t) STAGES * STAGE_BYTES + 256;
@@ -113,11 +116,15 @@ struct WgWarps {
     static constexpr int GW = IM2C ? 4 : 8, THREADS = 32 * (GW + 1 + (ISS2 ? 1 : 0));
 };
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB, bool ISS2 = false, int BKP = 64>
+// PAIR: clusters of two CTAs (x) share 256-row tiles through cta_group::2 MMAs issued by the even
+// CTA; each CTA loads its own A rows and half of the B columns (the odd CTA's loads complete on the
+// even CTA's barriers) and writes its own 128 rows of dW.
+template <int BN, int STAGES, bool XA, bool IM2C, int KB, bool ISS2 = false, int BKP = 64, bool PAIR = false>
 __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     tc_wgrad_kernel(const __grid_constant__ TcWgradParams p, const __grid_constant__ CUtensorMap dymap,
                     const __grid_constant__ CUtensorMap xmap) {
-    using C = WgCfg<BN, STAGES, XA, KB, BKP>;
+    using C = WgCfg<BN, STAGES, XA, KB, BKP, PAIR>;
+    static_assert(!PAIR || (IM2C && KB == 1 && !ISS2 && BKP == 128 && BN >= 128), "CTA pairs: 128-pixel chunks, 256 x 128 / 256");
     static_assert(BKP == 64 || (IM2C && KB == 1 && !ISS2), "128-pixel chunks: im2col path, one chunk per stage");
     static_assert(IM2C || KB == 1, "the cp.async gather fills one chunk per stage");
     static_assert(!ISS2 || (IM2C && KB == 2), "two issuers: alternate chunks of two-chunk stages");
@@ -144,21 +151,33 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
         tc::prefetch_tmap(&dymap);
         if (IM2C) tc::prefetch_tmap(&xmap);
     }
+    uint32_t prank = 0;   // rank in the CTA pair (0: the MMA-issuing CTA)
+    if constexpr (PAIR) {
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(prank));
+        prank &= 1;
+    }
     if (warp == GW) {
-        tc::tmem_alloc(tmem_holder, TCOLS);
-        tc::tmem_relinquish();
+        if constexpr (PAIR) {
+            tc::tmem_alloc_pair(tmem_holder, TCOLS);
+            tc::tmem_relinquish_pair();
+        } else {
+            tc::tmem_alloc(tmem_holder, TCOLS);
+            tc::tmem_relinquish();
+        }
     }
     tc::pdl_wait();   // no global memory access above
     tc::pdl_trigger();
     tc::tc_fence_before();
     __syncthreads();
+    if constexpr (PAIR) tc::cluster_sync();   // both CTAs' barriers exist before either signals the other
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_holder;
 
     // tile origins along the X extent (n = tap*Cp + ci) and the channel extent (co)
     const int mrow0 = blockIdx.x * C::BM, ncol0 = blockIdx.y * BN;
-    const int x0 = XA ? mrow0 : ncol0;
-    const int co0 = XA ? ncol0 : mrow0;
+    const int bhalf = PAIR ? (int) prank * C::BNL : 0;   // this CTA's B columns within the tile
+    const int x0 = XA ? mrow0 : ncol0 + bhalf;
+    const int co0 = XA ? ncol0 + bhalf : mrow0;
     const int chunk0 = blockIdx.z * p.chunks_per_split;
     const int KT = min(p.chunks_per_split, p.nchunks - chunk0);   // chunks of this split
     const int NG = (KT + KB - 1) / KB;                              // pipeline stages they fill
@@ -221,7 +240,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     constexpr int NBLK = 4 * (BN / 32);
     constexpr uint32_t RECV_MAX = (uint32_t) (NBLK + 7) * 4096u;
     constexpr bool PUSH_FITS = (size_t) STAGES * C::STAGE_BYTES >= (size_t) RECV_MAX + 4 * 8192;
-    const bool push = PUSH_FITS && p.cluster && p.xchg;
+    const bool push = !PAIR && PUSH_FITS && p.cluster && p.xchg;
 
     if (IM2C && warp < 4) {
         // one thread: im2col TMA for each 64-channel X atom (a fixed tap and channel chunk
@@ -240,12 +259,16 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
             }
             const uint32_t xoff = XA ? 0 : C::A_BYTES;
             const uint32_t dyoff = XA ? C::A_BYTES : 0;
+            // pairs: every load of both CTAs completes on the even CTA's full barrier
+            const uint32_t lead_full = PAIR ? tc::mapa_shared(tc::smem_u32(full), 0) : 0u;
             for (int g = 0; g < NG; g++) {
                 const int s = g % STAGES;
                 const uint32_t ph = (g / STAGES) & 1;
                 if (g >= STAGES && !(ok = tc::mbar_wait(&empty[s], ph ^ 1, p.err, 11))) break;
                 const int nch = min(KB, KT - g * KB);
-                tc::mbar_arrive_expect_tx(&full[s], nch * (C::X_ATOMS * C::ATOM_BYTES + C::DY_BYTES));
+                if (!PAIR || prank == 0)
+                    tc::mbar_arrive_expect_tx(&full[s], (PAIR ? 2 : 1) * nch * (C::X_ATOMS * C::ATOM_BYTES + C::DY_BYTES));
+                const uint32_t fb = lead_full + (uint32_t) s * 8u;
                 for (int c = 0; c < nch; c++) {
                     const int pbase = (chunk0 + g * KB + c) * C::BK;
                     uint32_t q, ow, oh, b;
@@ -255,15 +278,25 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                     const uint32_t st0 = tc::smem_u32(base + s * C::STAGE_BYTES + c * C::CHUNK_BYTES);
 #pragma unroll
                     for (int a = 0; a < C::X_ATOMS; a++) {
-                        if (p.x2d)   // one tap: the atom's channels are columns a_ci of the [P][Cp] matrix
-                            tc::tma_load_2d(st0 + xoff + a * C::ATOM_BYTES, &xmap, a_ci[a], pbase, &full[s]);
-                        else
-                            tc::tma_load_im2col_4d(st0 + xoff + a * C::ATOM_BYTES, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a],
-                                                   a_oy[a], &full[s]);
+                        const uint32_t d = st0 + xoff + a * C::ATOM_BYTES;
+                        if (PAIR) {
+                            if (p.x2d)
+                                tc::tma_load_2d_pair(d, &xmap, a_ci[a], pbase, fb);
+                            else
+                                tc::tma_load_im2col_4d_pair(d, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a], a_oy[a], fb);
+                        } else if (p.x2d) {   // one tap: the atom's channels are columns a_ci of the [P][Cp] matrix
+                            tc::tma_load_2d(d, &xmap, a_ci[a], pbase, &full[s]);
+                        } else {
+                            tc::tma_load_im2col_4d(d, &xmap, a_ci[a], w0, h0, (int) b, a_ox[a], a_oy[a], &full[s]);
+                        }
                     }
 #pragma unroll
-                    for (int a = 0; a < C::DY_ATOMS; a++)
-                        tc::tma_load_2d(st0 + dyoff + a * C::ATOM_BYTES, &dymap, co0 + 64 * a, pbase, &full[s]);
+                    for (int a = 0; a < C::DY_ATOMS; a++) {
+                        if (PAIR)
+                            tc::tma_load_2d_pair(st0 + dyoff + a * C::ATOM_BYTES, &dymap, co0 + 64 * a, pbase, fb);
+                        else
+                            tc::tma_load_2d(st0 + dyoff + a * C::ATOM_BYTES, &dymap, co0 + 64 * a, pbase, &full[s]);
+                    }
                 }
             }
         }
@@ -346,7 +379,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
         float *wrow = p.ws + ((size_t) blockIdx.z * Mext + m) * Next;
         if (push) {
             // the partial tile leaves TMEM after the cluster barrier below
-        } else if (p.cluster) {
+        } else if (!PAIR && p.cluster) {
             // this split's partial tile into shared memory (the ring is idle now), rows padded by
             // 4 floats against bank conflicts; the cluster adds the splits below
             float *R = reinterpret_cast<float *>(base);
@@ -454,8 +487,8 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
             }
         }
     } else if (warp == GW || (ISS2 && warp == GW + 1)) {
-        if (lane == 0) {
-            constexpr uint32_t idesc = tc::idesc_bf16(128, BN, 1, 1);
+        if (lane == 0 && (!PAIR || prank == 0)) {
+            constexpr uint32_t idesc = tc::idesc_bf16(PAIR ? 256 : 128, BN, 1, 1);
             const int j = warp - GW;   // issuer: chunk parity it takes (ISS2), accumulator
             const uint32_t dt = tmem + (uint32_t) (j * BN);
             for (int g = 0; g < NG; g++) {
@@ -475,12 +508,22 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
                     if (ISS2 && c != j) continue;
                     const uint64_t ad = ad0 + ((c * C::CHUNK_BYTES) >> 4), bd = ad + (C::A_BYTES >> 4);
 #pragma unroll
-                    for (int k = 0; k < C::BK / 16; k++)
-                        tc::mma_f16(dt, ad + 128 * k, bd + 128 * k, idesc, (g | (ISS2 ? 0 : c) | k) != 0);
+                    for (int k = 0; k < C::BK / 16; k++) {
+                        if constexpr (PAIR)
+                            tc::mma_f16_pair(dt, ad + 128 * k, bd + 128 * k, idesc, (g | c | k) != 0);
+                        else
+                            tc::mma_f16(dt, ad + 128 * k, bd + 128 * k, idesc, (g | (ISS2 ? 0 : c) | k) != 0);
+                    }
                 }
-                tc::mma_commit(&empty[s]);
+                if constexpr (PAIR)
+                    tc::mma_commit_pair(&empty[s], (uint16_t) 3);   // both CTAs' stage s is free
+                else
+                    tc::mma_commit(&empty[s]);
             }
-            tc::mma_commit(accum);
+            if constexpr (PAIR)
+                tc::mma_commit_pair(accum, (uint16_t) 3);
+            else
+                tc::mma_commit(accum);
         }
         __syncwarp();
     }
@@ -595,7 +638,7 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
             if (lane == 0) wg_bulk_wait_all();
             __syncwarp();
         }
-    } else if (p.cluster) {
+    } else if (!PAIR && p.cluster) {
         // dW = sum of the cluster's partial tiles in split (cluster rank) order; rank r adds rows
         // [r*rows, (r+1)*rows) across all ranks' shared memory and writes them.  With grouped
         // clusters (p.groups > 1) the slice goes to gws instead, and the last cluster of the
@@ -706,8 +749,14 @@ __global__ void __launch_bounds__(WgWarps<IM2C, ISS2>::THREADS, 1)
     }
     tc::tc_fence_before();
     __syncthreads();
+    if constexpr (PAIR) tc::cluster_sync();   // the pair's TMEM is released together
     tc::tc_fence_after();
-    if (warp == GW) tc::tmem_dealloc(tmem, TCOLS);
+    if (warp == GW) {
+        if constexpr (PAIR)
+            tc::tmem_dealloc_pair(tmem, TCOLS);
+        else
+            tc::tmem_dealloc(tmem, TCOLS);
+    }
 }
 
 // First pass of the reduction when there are many splits: group g sums the
@@ -794,11 +843,11 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false, int BKP = 64>
+template <int BN, int STAGES, bool XA, bool IM2C, int KB = 1, bool ISS2 = false, int BKP = 64, bool PAIR = false>
 cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUtensorMap &xmap, dim3 grid,
                       cudaStream_t st) {
-    using C = WgCfg<BN, STAGES, XA, KB, BKP>;
-    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2, BKP>;
+    using C = WgCfg<BN, STAGES, XA, KB, BKP, PAIR>;
+    auto kern = tc_wgrad_kernel<BN, STAGES, XA, IM2C, KB, ISS2, BKP, PAIR>;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) C::SMEM);
@@ -809,7 +858,7 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     // stream: launched without programmatic serialization, so that its grids do not
     // hold SMs early while the persistent chain kernels want them.
     constexpr int THREADS = WgWarps<IM2C, ISS2>::THREADS;
-    if (!p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(THREADS), C::SMEM, st, p, map, xmap);
+    if (!PAIR && !p.cluster) return cg_launch_ex(CG_PDL_OFF, kern, grid, dim3(THREADS), C::SMEM, st, p, map, xmap);
     // the splits of one tile as a cluster along z
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -818,9 +867,9 @@ cudaError_t launch_wg(const TcWgradParams &p, const CUtensorMap &map, const CUte
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = 1;
+    at[0].val.clusterDim.x = PAIR ? 2 : 1;   // pairs: adjacent M tiles (grid.x is even)
     at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = p.groups > 1 ? p.csize : grid.z;
+    at[0].val.clusterDim.z = PAIR ? 1 : (p.groups > 1 ? p.csize : grid.z);
     cfg.attrs = at;
     cfg.numAttrs = 1;
     cg_note_launch();
@@ -866,6 +915,14 @@ template <bool IM2C>
 cudaError_t launch_wg_any(const TcWgradParams &p, const CUtensorMap &dymap, const CUtensorMap &xmap, int bn, int xa,
                           dim3 grid, cudaStream_t st) {
     if constexpr (IM2C) {
+        if (p.pair) {   // CTA pairs, 128-pixel chunks: 256 x 256 tiles, 3 stages of 64 KB per CTA; 256 x 128, 4 x 48 KB
+            if ((bn != 128 && bn != 256) || (grid.x & 1)) return cudaErrorInvalidValue;
+            if (bn == 128)
+                return xa ? launch_wg<128, 4, true, IM2C, 1, false, 128, true>(p, dymap, xmap, grid, st)
+                          : launch_wg<128, 4, false, IM2C, 1, false, 128, true>(p, dymap, xmap, grid, st);
+            return xa ? launch_wg<256, 3, true, IM2C, 1, false, 128, true>(p, dymap, xmap, grid, st)
+                      : launch_wg<256, 3, false, IM2C, 1, false, 128, true>(p, dymap, xmap, grid, st);
+        }
         if (p.kb1) {   // one chunk per stage: 64-wide 4 stages of 24 KB, 128-wide 6 x 32 KB, 256-wide 4 x 48 KB
             if (xa) {
                 switch (bn) {
@@ -1016,7 +1073,8 @@ bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1, int is
                        : bn == 256 && cluster_fits<256, 4, false, false>(splits);
 }
 
-int tc_wgrad_stages(int bn, int im2col, int kb1, int wide) {
+int tc_wgrad_stages(int bn, int im2col, int kb1, int wide, int pair) {
+    if (im2col && pair) return bn == 128 ? 4 : 3;
     if (im2col && wide) return bn == 64 ? 4 : (bn == 128 ? 3 : 2);
     if (im2col) return kb1 ? (bn == 128 ? 6 : 4) : (bn == 128 ? 3 : 2);
     return bn == 128 ? 3 : 4;

@@ -42,6 +42,9 @@ struct TcWgradParams {
     // dW of the NHWC API ([ci][kh][kw][co], kn % 4 == 0, Cp % 32 == 0) as a 3-D FP32 tensor
     // (co, tap, ci) with 32 x 1 x 32 boxes and 128-byte swizzle: the single-split epilogue and
     // the one-cluster reduction stage 32 x 32 blocks in shared memory and write them by TMA
+    // CTA pairs (cluster x = 2, grid.x even): 256 x bn tiles (bn 128 / 256) through cta_group::2 MMAs,
+    // 128-pixel chunks; no split clusters (several splits go to ws)
+    int pair;
     int dw_tma;
     // with dw_tma and one cluster: the splits' partial tiles meet in ws ([tile][rank][32 x 32
     // blocks], 16-byte aligned) instead of distributed shared memory
@@ -59,7 +62,7 @@ cudaError_t tc_wgrad_launch(const TcWgradParams &p, const CUtensorMap &dymap, co
 // Whether splits (2..8) can run as clusters for this tile width / operand side / stage form.
 bool tc_wgrad_cluster_ok(int bn, int xa, int im2col, int splits, int kb1 = 0, int iss2 = 0, int wide = 0);
 // Ring stages of the general weight-gradient kernel for a tile width and form.
-int tc_wgrad_stages(int bn, int im2col, int kb1, int wide = 0);
+int tc_wgrad_stages(int bn, int im2col, int kb1, int wide = 0, int pair = 0);
 // Tile counters of the grouped cluster reduction on the current device: `n` consecutive
 // zero words for one launch (a rotating range of a fixed device array; NULL if unavailable).
 unsigned *tc_wgrad_counters(int n);

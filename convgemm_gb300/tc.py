@@ -127,6 +127,7 @@ WGRAD_SLAB = 0x80000        # stride-1 layers with 128-channel blocks: the slab 
 WGRAD_STAGES1 = 0x400000    # im2col path: one chunk per ring stage, twice the stages
 WGRAD_TWO_ISSUERS = 0x800000  # im2col path, two chunks per stage: a second MMA-issuing warp
 WGRAD_WIDE_CHUNKS = 0x1000000  # im2col path: 128-pixel chunks, one per stage (TMA boxes of twice the bytes)
+WGRAD_PAIR = 0x2000000      # im2col path: CTA pairs sharing 256 x 256 / 256 x 128 tiles (cta_group::2 MMAs)
 CONV_STAGES1 = 16           # forward / input-gradient aux: one K block per ring stage, twice the stages
 
 

@@ -292,6 +292,11 @@ convgemm_status_t convgemm_tune_set(int op, const convgemm_shape_t *shape, int b
  * box carries twice the bytes (the per-box cost, not the bytes, bounds a TMA stream of 8 KB
  * boxes); the MMAs run in the same order, so dW is bit-identical to the default's. */
 #define CONVGEMM_WGRAD_WIDE_CHUNKS 0x1000000
+/* im2col path: CTA pairs (thread-block clusters of two) share 256 x 256 (bn 256, the default) or
+ * 256 x 128 (bn 128) tiles through cta_group::2 MMAs, each CTA loading its A rows and half of the
+ * B columns (128-pixel chunks); several splits reduce through the workspace.  Other FP32 orders
+ * than the default: reproducible, within FP32 accumulation. */
+#define CONVGEMM_WGRAD_PAIR 0x2000000
 #define CONVGEMM_WGRAD_GROUPS(csize) ((csize) == 8 ? 0x300000 : (csize) == 4 ? 0x200000 : (csize) == 2 ? 0x100000 : 0)
 void convgemm_tune_clear(void);
 /* What the tuning table (or the heuristic) selects for the forward, input gradient or weight

@@ -207,7 +207,7 @@ def test_shipped_tuning_table_entries_parse():
         assert e["bn"] in (0, 64, 128, 256), k
         aux = int(e["splits"])
         if op == "wgrad":
-            assert aux >= 0 and (aux & ~0x1FBFFFF) == 0, k
+            assert aux >= 0 and (aux & ~0x3FBFFFF) == 0, k
         else:
             assert (aux & ~24) in (0, 1, 2, 5, 6), k
         assert e["kernel"] in (0, 1, 2), k

@@ -572,6 +572,50 @@ def test_wgrad_tma_epilogue_matches_scalar_layout(cglib, b, h, w, c, kn, k, st, 
     assert torch.equal(nhwc, nchw)
 
 
+@pytest.mark.parametrize("b,h,w,c,kn,k,st,pad,xa", [
+    (8, 7, 7, 256, 256, 3, 1, 1, 0),       # dY on A: 2 M tiles (one pair), 9 N tiles
+    (4, 14, 14, 128, 384, 1, 1, 0, 0),     # 1x1 tiled X boxes, 3 M tiles padded to 4, N tile past Nx
+    (4, 9, 9, 192, 256, 3, 1, 1, 1),       # X on A: 14 M tiles (the last one partly past Nx)
+    (8, 10, 12, 128, 320, 3, 2, 1, 1),     # strided, X on A, 320 channels: second N tile partly past kn
+])
+def test_wgrad_cta_pairs(cglib, oracle_lib, b, h, w, c, kn, k, st, pad, xa):
+    """CTA pairs (cta_group::2 MMAs on 256 x 256 and 256 x 128 tiles, each CTA loading its A rows and
+    half of the B columns):
+    within FP32 accumulation of FP64 on the same BF16 inputs, bit-reproducible, and the NHWC (TMA
+    store) and NCHW (element stores) results hold the same bits, for one split and for several."""
+    from convgemm_gb300 import tc
+    cg, O = cglib, oracle_lib
+    s = cg.Shape.of(b, h, w, c, kn, k, k, pad, pad, st, st)
+    g = C.geom(b, h, w, c, kn, k, k, stride=st, pad=pad)
+    ho, wo = C.out_hw(g)
+    rng = np.random.default_rng(31 + c + kn + k)
+    x = rng.standard_normal(b * h * w * c).astype(np.float32)
+    dy = rng.standard_normal(b * ho * wo * kn).astype(np.float32)
+    xd = to_dev_bf16_nhwc(cg, tc, x, b, c, h, w)
+    dyd = to_dev_bf16_nhwc(cg, tc, dy, b, kn, ho, wo)
+    ref = O.wgrad_f64(C.NHWC, g, bf16r(dy), bf16r(x))
+    try:
+        for bn, splits in ((256, 1), (256, 3), (128, 1), (128, 3)):
+            tc.tune_set(tc.TUNE_WGRAD, s, bn, splits | tc.WGRAD_PAIR | (tc.WGRAD_X_ON_A if xa else 0))
+            kern, bnd, stages, cl = tc.tune_describe(tc.TUNE_WGRAD, s)
+            assert (kern, bnd, stages, cl) == (0, bn, 3 if bn == 256 else 4, 2)
+            _, sp, mx = tc.wgrad_bf16_plan(s)
+            assert 1 <= sp <= splits and (sp > 1) == (splits > 1 and mx > 1), (sp, mx)
+            ws = torch.empty(tc.wgrad_bf16_workspace_size(s) // 4 + 1, device="cuda")
+            out = []
+            for layout in (cg.NHWC, cg.NHWC, cg.NCHW):
+                d = torch.full((c * k * k * kn,), float("nan"), device="cuda")
+                tc.wgrad_bf16(layout, s, dyd, xd, d, ws)
+                out.append(d)
+            torch.cuda.synchronize()
+            cg.check_device()
+            assert torch.equal(out[0], out[1]), (bn, splits)
+            assert torch.equal(out[0].view(c, k * k, kn).permute(2, 0, 1).contiguous(), out[2].view(kn, c, k * k)), (bn, splits)
+            assert rel_max_rms(out[0].cpu().numpy(), ref)[0] <= 1e-4, (bn, splits)
+    finally:
+        tc.tune_clear()
+
+
 def test_grouped_preparation_matches_per_layer_calls(cglib):
     """One grouped launch of folds and packings gives the bytes of the per-layer calls."""
     from convgemm_gb300 import tc
