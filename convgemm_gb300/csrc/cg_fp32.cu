@@ -16,7 +16,20 @@
 // reduction slices of 8 double-buffered through shared memory.  The running
 // sum of completed KC blocks lives in shared memory (it is touched once per
 // 384 reduction steps).
+//
+// Block split: when a convolution's tiles fill less than the GPU (the 14x14 and 7x7
+// layers), the forward and input gradient run one CTA per (tile, reduction segment):
+// each CTA writes the FMA chain of one KC block (input gradient: one KC block of one
+// tap) to a scratch plane, and a second kernel adds the planes in order and applies
+// the epilogue.  The chains start from +0 and so are never -0, hence 0 + chain ==
+// chain and the ordered sum of the planes equals the running sum of the fused form
+// bit for bit.
 #include <climits>
+#include <type_traits>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
 #include "cg_common.cuh"
 
 namespace {
@@ -51,6 +64,7 @@ struct FwdOp {
     float *y;
     cg_epi e;
     FastDiv dwo, dho, dkw, dkh;
+    float *ws;   // block split: [K blocks][P][kn] chains, else NULL
 
     __host__ __device__ int M() const { return (int) g.P; }
     __host__ __device__ int N() const { return g.kn; }
@@ -94,12 +108,25 @@ struct FwdOp {
         size_t o = nchw ? ((size_t) cl.n * g.K + ri.r) : ((size_t) ri.r * g.kn + cl.n);
         return __ldg(w + o);
     }
-    __device__ void range(int z, int &rbeg, int &rend) const { rbeg = 0; rend = g.K; }
+    __host__ __device__ int segments() const { return (g.K + KC - 1) / KC; }
+    __device__ void range(int z, int &rbeg, int &rend) const {
+        if (ws) {
+            rbeg = z * KC;
+            rend = min(g.K, rbeg + KC);
+        } else {
+            rbeg = 0;
+            rend = g.K;
+        }
+    }
     __device__ int next_fold(int r, int rend) const {
         int nf = (r / KC + 1) * KC;
         return nf >= rend ? INT_MAX : nf;
     }
     __device__ float s_init(int m, int n) const { return 0.0f; }
+    __device__ void finish_z(int z, int m, int n, float s) const {
+        if (!ws) return finish(m, n, s);
+        if (m < (int) g.P && n < g.kn) ws[((size_t) z * g.P + m) * g.kn + n] = s;
+    }
     __device__ void finish(int m, int n, float s) const {
         if (m >= (int) g.P || n >= g.kn) return;
         float v = fwd_epilogue(s, n, e);
@@ -194,6 +221,7 @@ struct DgradOp {
     const float *w, *dy;
     float *dx;
     FastDiv dw_, dh_, dkn, dkw, dvs, dhs;
+    float *ws;   // block split: [segment][b*h*w][c] chains (segment = tap, KC block of kn), else NULL
 
     __host__ __device__ int M() const { return g.b * g.h * g.w; }
     __host__ __device__ int N() const { return g.c; }
@@ -241,7 +269,17 @@ struct DgradOp {
         size_t o = nchw ? ((size_t) ri.l * g.K + k) : (k * g.kn + ri.l);
         return __ldg(w + o);
     }
-    __device__ void range(int z, int &rbeg, int &rend) const { rbeg = 0; rend = g.kh * g.kw * g.kn; }
+    __host__ __device__ int segments() const { return g.kh * g.kw * ((g.kn + KC - 1) / KC); }
+    __device__ void range(int z, int &rbeg, int &rend) const {
+        if (ws) {
+            const int nch = (g.kn + KC - 1) / KC, tap = z / nch, j = z - tap * nch;
+            rbeg = tap * g.kn + j * KC;
+            rend = tap * g.kn + min(g.kn, (j + 1) * KC);
+        } else {
+            rbeg = 0;
+            rend = g.kh * g.kw * g.kn;
+        }
+    }
     __device__ int next_fold(int r, int rend) const {
         uint32_t tap, l;
         dkn.divmod(r, tap, l);
@@ -256,8 +294,16 @@ struct DgradOp {
         return (((size_t) bb * g.c + n) * g.h + ih) * g.w + iw;
     }
     __device__ float s_init(int m, int n) const {
+        if (ws || !accumulate || m >= M() || n >= g.c) return 0.0f;   // split: the reduction starts from dx
+        return dx[out_index(m, n)];
+    }
+    __device__ float s_start(int m, int n) const {
         if (!accumulate || m >= M() || n >= g.c) return 0.0f;
         return dx[out_index(m, n)];
+    }
+    __device__ void finish_z(int z, int m, int n, float s) const {
+        if (!ws) return finish(m, n, s);
+        if (m < M() && n < g.c) ws[((size_t) z * M() + m) * g.c + n] = s;
     }
     __device__ void finish(int m, int n, float s) const {
         if (m >= M() || n >= g.c) return;
@@ -265,8 +311,6 @@ struct DgradOp {
     }
 };
 
-template <class Op> struct has_finish_z { static constexpr bool value = false; };
-template <> struct has_finish_z<WgradOp> { static constexpr bool value = true; };
 
 template <class Op>
 __global__ void __launch_bounds__(NT) fp32_igemm_kernel(const Op op) {
@@ -366,9 +410,32 @@ __global__ void __launch_bounds__(NT) fp32_igemm_kernel(const Op op) {
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             const float s = Ssm[(i * 8 + j) * NT + tid];
-            if constexpr (has_finish_z<Op>::value) op.finish_z(z, mrow(i), ncol(j), s);
-            else op.finish(mrow(i), ncol(j), s);
+            op.finish_z(z, mrow(i), ncol(j), s);
         }
+}
+
+// Block split: out(m, n) = finish(((start + ws[0]) + ws[1]) + ...), the planes in segment order
+// (start: 0, or dx for the accumulating input gradient).
+template <class Op>
+__global__ void fp32_split_reduce_kernel(const Op op, const float *__restrict__ ws, int nz, int M, int N) {
+    const long long total = (long long) M * N;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x) {
+        const int m = (int) (i / N), n = (int) (i % N);
+        float s;
+        if constexpr (std::is_same<Op, DgradOp>::value) s = op.s_start(m, n);
+        else s = 0.0f;
+        int z = 0;
+        for (; z + 8 <= nz; z += 8) {
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = ws[(size_t) (z + j) * total + i];
+#pragma unroll
+            for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
+        }
+        for (; z < nz; z++) s = __fadd_rn(s, ws[(size_t) z * total + i]);
+        op.finish(m, n, s);
+    }
 }
 
 // dW(m, n) = ((ws[0] + ws[1]) + ws[2]) + ... : the reference's block order.
@@ -408,6 +475,59 @@ cudaError_t launch(const Op &op, int gz, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Scratch planes of the block split, one grow-only buffer per (device, stream): a CUDA graph
+// that captured a buffer keeps using it, so buffers are never freed or reused for another stream.
+std::mutex g_split_mu;
+std::map<std::pair<int, cudaStream_t>, std::pair<float *, size_t>> g_split_ws;
+constexpr size_t SPLIT_WS_MAX = (size_t) 256 << 20;
+
+float *split_scratch(size_t bytes, cudaStream_t st) {
+    if (bytes > SPLIT_WS_MAX) return nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_split_mu);
+    auto &e = g_split_ws[{dev, st}];
+    if (e.second >= bytes) return e.first;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;   // no allocation under capture: the fused form runs instead
+    }
+    size_t want = e.second ? e.second : ((size_t) 32 << 20);
+    while (want < bytes) want *= 2;
+    if (want > SPLIT_WS_MAX) want = SPLIT_WS_MAX;
+    float *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    e = {p, want};   // the previous buffer stays allocated for graphs that captured it
+    return p;
+}
+
+// The block split pays when the fused grid leaves SMs idle (two 128x128 CTAs fit per SM).
+template <class Op>
+cudaError_t launch_split_or_fused(Op op, int M, int N, cudaStream_t st) {
+    const long long tiles = (long long) ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int nz = op.segments();
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    op.ws = nullptr;
+    if (nz > 1 && tiles < 2LL * sms) {
+        const size_t bytes = sizeof(float) * (size_t) nz * (size_t) M * (size_t) N;
+        op.ws = split_scratch(bytes, st);
+    }
+    if (!op.ws) return launch(op, 1, st);
+    cudaError_t e = launch(op, nz, st);
+    if (e != cudaSuccess) return e;
+    const long long total = (long long) M * N;
+    const int blocks = (int) std::min<long long>((total + 255) / 256, (long long) sms * 16);
+    float *ws = op.ws;
+    fp32_split_reduce_kernel<Op><<<blocks, 256, 0, st>>>(op, ws, nz, M, N); cg_note_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float *x, float *y,
@@ -423,7 +543,8 @@ cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float
     op.dho = FastDiv(op.g.ho);
     op.dkw = FastDiv(s.kw);
     op.dkh = FastDiv(s.kh);
-    return launch(op, 1, st);
+    op.ws = nullptr;
+    return launch_split_or_fused(op, (int) op.g.P, op.g.kn, st);
 }
 
 size_t cg_fp32_wgrad_ws_bytes(const cg_shape &s) {
@@ -469,5 +590,6 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     op.dkw = FastDiv(s.kw);
     op.dvs = FastDiv(s.vstride);
     op.dhs = FastDiv(s.hstride);
-    return launch(op, 1, st);
+    op.ws = nullptr;
+    return launch_split_or_fused(op, op.M(), op.g.c, st);
 }

@@ -126,6 +126,34 @@ def test_random_shapes_against_restatement(cglib, oracle_lib, seed):
                 assert bitexact(got, want), (g, layout, op)
 
 
+@pytest.mark.parametrize("b,h,w,c,kn", [
+    (2, 7, 7, 512, 512),     # 4 tiles: one CTA per (tile, KC block), 12 blocks, ordered reduction
+    (4, 56, 56, 64, 512),    # 392 tiles: the fused form, 2 KC blocks folded in the kernel
+])
+def test_block_split_and_fused_forms_follow_reference_order(cglib, oracle_lib, b, h, w, c, kn):
+    """Small grids run the forward and input gradient one CTA per reduction segment and add the
+    segments in order in a second kernel; large grids fold them inside one kernel.  The forward
+    keeps the reference's bits in both forms (both layouts, with the epilogue); the input gradient,
+    plain and accumulating, stays within FP32 tolerance of the port."""
+    g = C.geom(b, h, w, c, kn, 3, 3, pad=1)
+    rng = np.random.default_rng(b * 1000 + kn)
+    K = 9 * c
+    inp = {"x": rng.uniform(-1, 1, b * h * w * c).astype(np.float32),
+           "w": (rng.standard_normal(K * kn) * np.sqrt(2 / K)).astype(np.float32),
+           "dy": rng.uniform(-1, 1, b * h * w * kn).astype(np.float32),
+           "dx0": rng.uniform(-1, 1, b * h * w * c).astype(np.float32),
+           "epi": {"bias": rng.uniform(-.1, .1, kn).astype(np.float32), "relu": True}}
+    for layout in (C.NHWC, C.NCHW):
+        n = b * h * w * kn
+        got = dropin(cglib, "fwd", layout, g, inp, np.zeros(n, np.float32), to_dev=True)
+        assert bitexact(got, port(oracle_lib, "fwd", layout, g, inp, n)), layout
+        got = dropin(cglib, "dgrad", layout, g, inp, inp["dx0"].copy(), to_dev=True)
+        want = port(oracle_lib, "dgrad", layout, g, inp, None)
+        assert errors(got, want)[0] <= FP32_TOL, layout
+        again = dropin(cglib, "dgrad", layout, g, inp, inp["dx0"].copy(), to_dev=True)
+        assert bitexact(got, again), layout
+
+
 def test_extended_api_streams_and_determinism(cglib):
     """convgemm_*_f32 on a side stream; weight and input gradients are bit-reproducible."""
     cg = cglib
