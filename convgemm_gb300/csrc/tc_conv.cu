@@ -44,6 +44,7 @@ using bf16 = __nv_bfloat16;
 constexpr int MODE_BF16 = 0;  // BF16 x BF16, kind::f16
 constexpr int MODE_FP8 = 1;   // E4M3 x E4M3, kind::f8f6f4 (64-byte K rows, 64-byte swizzle)
 constexpr int MODE_X3 = 2;    // 3xBF16: hi*hi + hi*lo + lo*hi into one accumulator, FP32 output
+constexpr int MODE_FP8W = 3;  // E4M3 with 128-channel K blocks: 128-byte K rows, 128-byte swizzle
 
 // KB 64-deep K blocks per pipeline stage: one full barrier and one MMA commit
 // cover KB blocks (a barrier round trip costs ~400 cycles, a 128 x 64 x 64 block
@@ -56,7 +57,7 @@ constexpr int MODE_X3 = 2;    // 3xBF16: hi*hi + hi*lo + lo*hi into one accumula
 // latency chain (TMEM load, scale/shift, convert, staging) rather than the MMAs.
 template <int BN, int STAGES, int KB = 1, int MODE = MODE_BF16, int MT = 1, int EW = 4>
 struct TcCfg {
-    static constexpr int BM = 128, BK = 64;            // K elements per block
+    static constexpr int BM = 128, BK = MODE == MODE_FP8W ? 128 : 64;   // K elements per block
     static constexpr int ROWB = MODE == MODE_FP8 ? 64 : 128;  // bytes of one K row of a block
     static constexpr int NOPS = MODE == MODE_X3 ? 2 : 1;      // hi / lo copies of each operand
     static constexpr uint32_t A_TILE = BM * ROWB;
@@ -269,7 +270,7 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                                                    offy, &full[s]);
                             tc::tma_load_2d(bb + C::B_TILE, &amaps.wlo, kcol, tl.n0, &full[s]);
                         }
-                        ci0 += 64;
+                        ci0 += C::BK;
                         if (ci0 == p.Cin) {
                             ci0 = 0;
                             tap++;
@@ -583,7 +584,8 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
             // issuer `me`: its M tile (MT = 2) or N half (MT = 1) when SPLIT, else everything
             const int me = (SPLIT && warp == C::ISS2_WARP) ? 1 : 0;
             constexpr int NI = (SPLIT && MT == 1) ? BN / 2 : BN;   // N of one MMA instruction
-            constexpr uint32_t idesc = MODE == MODE_FP8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, NI, 0, 0);
+            constexpr bool F8 = MODE == MODE_FP8 || MODE == MODE_FP8W;
+            constexpr uint32_t idesc = F8 ? tc::idesc_e4m3(128, BN) : tc::idesc_bf16(128, NI, 0, 0);
             const uint32_t n_off = (SPLIT && MT == 1) ? (uint32_t) (me * NI) : 0u;   // accumulator column
             const uint64_t b_off = (SPLIT && MT == 1) ? (uint64_t) (me * NI * C::ROWB) >> 4 : 0u;   // B rows
             uint32_t it = 0, lt = 0;
@@ -624,7 +626,7 @@ __global__ void __launch_bounds__(EW == 8 ? 384 : 288, 1)
                             if (SPLIT && MT == 2 && mt != me) continue;
                             const uint64_t ad = ad0 + (((kb * MT + mt) * C::A_BLOCK + k * 32) >> 4);
                             const uint32_t dtm = dt + (uint32_t) (mt * BN) + n_off;
-                            if (MODE == MODE_FP8) {
+                            if (F8) {
                                 tc::mma_f8(dtm, ad, bd, idesc, acc);
                             } else {
                                 tc::mma_f16(dtm, ad, bd, idesc, acc);
@@ -688,6 +690,14 @@ cudaError_t tc_conv_launch(const TcConvParams &p, const CUtensorMap &wmap, const
             case 64: return launch_bn<64, 4, 4, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
             case 128: return launch_bn<128, 3, 4, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
             case 256: return launch_bn<256, 3, 2, true, MODE_FP8>(p, wmap, omap, amaps, grid, st);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+    if (p.mode == MODE_FP8W) {   // 128-channel blocks: 16 KB per 128-row block, as BF16
+        switch (p.bn) {
+            case 64: return launch_bn<64, 4, 2, true, MODE_FP8W>(p, wmap, omap, amaps, grid, st);
+            case 128: return launch_bn<128, 3, 2, true, MODE_FP8W>(p, wmap, omap, amaps, grid, st);
+            case 256: return launch_bn<256, 3, 1, true, MODE_FP8W>(p, wmap, omap, amaps, grid, st);
             default: return cudaErrorInvalidValue;
         }
     }

@@ -89,7 +89,8 @@ convgemm_status_t tc_make_map_nd_dt(CUtensorMap *map, CUtensorMapDataType dt, in
 }
 
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
-                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes) {
+                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes,
+                                     int chans) {
     EncodeIm2colFn fn = encode_im2col_fn();
     if (!fn) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col is unavailable");
     if (((uintptr_t) ptr & 15) || (C * elem_bytes) % 16)
@@ -100,11 +101,12 @@ convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, i
     int lower[2] = {lo_w, lo_h};
     int upper[2] = {up_w, up_h};
     cuuint32_t estr[4] = {1, (cuuint32_t) sw, (cuuint32_t) sh, 1};
-    // 64 channels per pixel: 128 B rows (BF16, 128-byte swizzle) or 64 B rows (E4M3, 64-byte swizzle)
+    // `chans` channels per pixel: 128 B rows (64 BF16 or 128 E4M3, 128-byte swizzle) or 64 B rows
+    // (64 E4M3, 64-byte swizzle)
     CUresult r = fn(map, elem_bytes == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
-                    const_cast<void *>(ptr), dims, strides, lower, upper, 64, (cuuint32_t) pixels, estr,
+                    const_cast<void *>(ptr), dims, strides, lower, upper, (cuuint32_t) chans, (cuuint32_t) pixels, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    elem_bytes == 1 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                    chans * elem_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cg_set_error(CONVGEMM_ERROR_CUDA, "cuTensorMapEncodeIm2col failed (%d)", (int) r);
     return CONVGEMM_SUCCESS;
@@ -365,6 +367,16 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     if (mode != 0 && !p.im2col)
         return cg_set_error(CONVGEMM_ERROR_NOT_SUPPORTED,
                             "FP8 / 3xBF16 forms need channels a multiple of 64 (im2col-mode TMA)");
+    // E4M3 with channels a multiple of 128: 128-channel K blocks (128-byte rows and swizzle, one
+    // 16 KB box per 128-row block and four 32-deep MMAs per block, as BF16) instead of 64-byte rows
+    bool f8w = mode == 1 && p.im2col && pl.Cin % 128 == 0 && pl.Ktot % 128 == 0;
+    for (int c = 0; f8w && c < pi.ncls; c++)
+        if (pi.cls[c].kbeg % 128 || pi.cls[c].ktiles % 2) f8w = false;
+    if (f8w) {
+        if (convgemm_status_t e = tc_make_map_2d_sw(&wmap, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, wpacked, pl.Cout, pl.Ktot,
+                                                    128, p.bn, CU_TENSOR_MAP_SWIZZLE_128B))
+            return e;
+    }
     if (p.im2col) {
         p.cpb = pl.Cin / 64;
         for (int c = 0; c < pi.ncls; c++) {
@@ -372,11 +384,11 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
             const int up_y = cl.lo_y + (cl.Hg - 1) * cl.isy - (pl.Hin - 1);
             const int up_x = cl.lo_x + (cl.Wg - 1) * cl.isx - (pl.Win - 1);
             if (convgemm_status_t e = tc_make_im2col_map(&amaps.a[c], in, s.b, pl.Hin, pl.Win, pl.Cin, cl.lo_y,
-                                                         cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, eb))
+                                                         cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, eb, f8w ? 128 : 64))
                 return e;
             if (mode == 2)
                 if (convgemm_status_t e = tc_make_im2col_map(&amaps.alo[c], in_lo, s.b, pl.Hin, pl.Win, pl.Cin,
-                                                             cl.lo_y, cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, 2))
+                                                             cl.lo_y, cl.lo_x, up_y, up_x, cl.isy, cl.isx, 128, 2, 64))
                     return e;
         }
         if (mode == 2)
@@ -404,8 +416,10 @@ convgemm_status_t tc_run(const TcPlan &pl, const cg_shape &s, const void *in, co
     // four epilogue warps, 64 / 128-wide tiles)
     p.kb1 = (aux_override & 16) && mode == 0 && p.im2col && p.mt == 1 && p.ew == 4 && !stats && p.bn != 256;
     int t0 = 0, g0 = 0;
+    if (f8w) p.mode = 3;   // MODE_FP8W: the classes count 128-channel K blocks
     for (int c = 0; c < pl.ncls; c++) {
         p.cls[c] = pi.cls[c];
+        if (f8w) p.cls[c].ktiles /= 2;
         p.cls[c].tile0 = t0;
         p.cls[c].gbase = g0;   // statistics groups of 32 rows, classes concatenated
         t0 += (pl.cls[c].mtiles + p.mt - 1) / p.mt * p.ntiles;
@@ -838,7 +852,7 @@ extern "C" convgemm_status_t convgemm_wgrad_bf16(convgemm_layout_t layout, const
                 return e;
         } else if (p.im2col) {
             if (convgemm_status_t e = tc_make_im2col_map(&xmap, x, s.b, s.h, s.w, p.Cp, -s.vpad, -s.hpad, up_h, up_w,
-                                                         s.vstride, s.hstride, w.bk, 2))
+                                                         s.vstride, s.hstride, w.bk, 2, 64))
                 return e;
         }
     }

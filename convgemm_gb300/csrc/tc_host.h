@@ -24,7 +24,8 @@ convgemm_status_t tc_make_map_2d(CUtensorMap *map, CUtensorMapDataType dt, int e
 convgemm_status_t tc_make_map_2d_sw(CUtensorMap *map, CUtensorMapDataType dt, int elem_bytes, const void *ptr,
                                     long long rows, long long cols, int box_cols, int box_rows, CUtensorMapSwizzle sw);
 convgemm_status_t tc_make_im2col_map(CUtensorMap *map, const void *ptr, int B, int H, int W, int C, int lo_h,
-                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes);
+                                     int lo_w, int up_h, int up_w, int sh, int sw, int pixels, int elem_bytes,
+                                     int chans = 64);
 bool tc_plan_im2col(TcPlan &pl);
 // BF16 tiled tensor map of any rank (<= 5): dims / box / element strides innermost first,
 // strides_bytes of dims 1.. ; 128-byte swizzle or none.
