@@ -12,10 +12,14 @@
 // One templated kernel serves every operation; an "op" object supplies the
 // implicit operands (im2row/im2col gathers straight from the activation
 // tensor, never materialised), the block boundaries of the reduction and the
-// store.  Tiles are 128x128 outputs per 256-thread CTA, 8x8 per thread,
-// reduction slices of 8 double-buffered through shared memory.  The running
-// sum of completed KC blocks lives in shared memory (it is touched once per
-// 384 reduction steps).
+// store.  Tiles are 128x128 outputs per 256-thread CTA (256x64 when the
+// operation has at most 64 columns), 8x8 per thread, reduction slices of 8
+// double-buffered through shared memory.  Every gather address splits into a
+// row part (computed once per thread) and a reduction-index part, which the
+// CTA tabulates in shared memory 256 indices at a time, so a gathered element
+// costs a table read, two bounds tests and an add.  The running sum of
+// completed KC blocks lives in shared memory (it is touched once per 384
+// reduction steps).
 //
 // Block split: when a convolution's tiles fill less than the GPU (the 14x14 and 7x7
 // layers), the forward and input gradient run one CTA per (tile, reduction segment):
@@ -25,6 +29,9 @@
 // chain and the ordered sum of the planes equals the running sum of the fused form
 // bit for bit.
 #include <climits>
+#include <cmath>
+#include <cstdint>
+#include <tuple>
 #include <type_traits>
 #include <map>
 #include <mutex>
@@ -34,8 +41,9 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 8, NT = 256;
+constexpr int BK = 8, NT = 256;
 constexpr int KC = 384;
+constexpr int OUT = 1 << 29;  // an input offset that puts a gather outside every image
 constexpr int SREGS = 64;  // outputs per thread
 constexpr size_t S_SMEM_BYTES = sizeof(float) * SREGS * NT;
 
@@ -57,9 +65,17 @@ __device__ __forceinline__ float fwd_epilogue(float t, int n, const cg_epi &e) {
 // ---------------------------------------------------------------- forward
 // GEMM rows m = output pixel p = (b*ho + ox)*wo + oy, columns n = output
 // channel, reduction r = K index (c, kx, ky).
+//
+// Every gather is base(row) + delta(r) in both layouts, valid where the input
+// position (ix(row) + ox(r), iy(row) + oy(r)) lies inside the image:
+//   NHWC  ((b*h + ix)*w + iy)*c + ch = ((b*h + bix)*w + biy)*c + ((kx*vdil)*w + ky*hdil)*c + ch
+//   NCHW  ((b*c + ch)*h + ix)*w + iy = ((b*c*h) + bix)*w + biy + (ch*h + kx*vdil)*w + ky*hdil
+// The row part is computed once per thread, the r part once per CTA (the
+// reduction-index table).
 struct FwdOp {
     ConvGeom g;
-    int nchw;
+    int nchw;        // layout of y
+    int xl, wl;      // layout of the x the kernel reads (0 NHWC, 1 NCHW) and of w (0 [K][kn], 1 [kn][K])
     const float *w, *x;
     float *y;
     cg_epi e;
@@ -69,46 +85,45 @@ struct FwdOp {
     __host__ __device__ int M() const { return (int) g.P; }
     __host__ __device__ int N() const { return g.kn; }
 
-    struct Row { int valid, bb, bix, biy; };
+    struct Row { long long base; int ix, iy; };
     __device__ Row row(int m) const {
-        Row rw;
-        rw.valid = m < (int) g.P;
         uint32_t q, oy, ox, bb;
-        dwo.divmod(rw.valid ? m : 0, q, oy);
+        dwo.divmod(m < g.P ? m : 0, q, oy);
         dho.divmod(q, bb, ox);
-        rw.bb = bb;
-        rw.bix = ox * g.vstr - g.vpad;
-        rw.biy = oy * g.hstr - g.hpad;
+        Row rw;
+        const int bix = (int) ox * g.vstr - g.vpad, biy = (int) oy * g.hstr - g.hpad;
+        rw.base = xl ? ((long long) bb * g.c * g.h + bix) * g.w + biy
+                     : (((long long) bb * g.h + bix) * g.w + biy) * g.c;
+        rw.ix = m < g.P ? bix : -OUT;
+        rw.iy = biy;
         return rw;
     }
-    struct Col { int valid, n; };
-    __device__ Col col(int n) const { return Col{n < g.kn, n}; }
-    struct RI { int valid, c, offx, offy, r; };
-    __device__ RI rinfo(int r, int rend) const {
-        RI ri;
-        ri.valid = r < rend;
-        ri.r = r;
-        uint32_t t, ky, kx, c;
-        dkw.divmod(ri.valid ? r : 0, t, ky);
-        dkh.divmod(t, c, kx);
-        ri.c = c;
-        ri.offx = kx * g.vdil;
-        ri.offy = ky * g.hdil;
-        return ri;
+    // Single-tap NHWC: the row's reduction indices are its input pixel's channels, contiguous.
+    __device__ bool row_in(const Row &rw) const { return in_range(rw.ix, g.h) && in_range(rw.iy, g.w); }
+    __device__ const float *asrc() const { return x; }
+    struct Col { long long base; int valid; };
+    __device__ Col col(int n) const { return Col{wl ? (long long) n * g.K : (long long) n, n < g.kn}; }
+    struct alignas(16) REnt { int delta, ox, oy, bd; };
+    __device__ REnt rent(int r, int rend) const {
+        uint32_t q, ky, kx, c;
+        dkw.divmod(r < rend ? r : 0, q, ky);
+        dkh.divmod(q, c, kx);
+        REnt t;
+        const int offx = (int) kx * g.vdil;
+        t.oy = (int) ky * g.hdil;
+        t.delta = xl ? ((int) c * g.h + offx) * g.w + t.oy : (offx * g.w + t.oy) * g.c + (int) c;
+        t.ox = r < rend ? offx : -OUT;
+        t.bd = r < rend ? (wl ? r : r * g.kn) : -1;
+        return t;
     }
-    __device__ float a(const Row &rw, const RI &ri) const {
-        int ix = rw.bix + ri.offx, iy = rw.biy + ri.offy;
-        if (!(rw.valid && ri.valid && in_range(ix, g.h) && in_range(iy, g.w))) return 0.0f;
-        size_t o = nchw ? ((((size_t) rw.bb * g.c + ri.c) * g.h + ix) * g.w + iy)
-                        : ((((size_t) rw.bb * g.h + ix) * g.w + iy) * g.c + ri.c);
-        return __ldg(x + o);
+    __device__ float a(const Row &rw, const REnt &t) const {
+        return in_range(rw.ix + t.ox, g.h) && in_range(rw.iy + t.oy, g.w) ? __ldg(x + (rw.base + t.delta)) : 0.0f;
     }
-    __device__ float b(const Col &cl, const RI &ri) const {
-        if (!(cl.valid && ri.valid)) return 0.0f;
-        size_t o = nchw ? ((size_t) cl.n * g.K + ri.r) : ((size_t) ri.r * g.kn + cl.n);
-        return __ldg(w + o);
+    __device__ float b(const Col &cl, const REnt &t) const {
+        return cl.valid && t.bd >= 0 ? __ldg(w + (cl.base + t.bd)) : 0.0f;
     }
     __host__ __device__ int segments() const { return (g.K + KC - 1) / KC; }
+    __host__ __device__ long long rlen() const { return g.K; }
     __device__ void range(int z, int &rbeg, int &rend) const {
         if (ws) {
             rbeg = z * KC;
@@ -144,57 +159,57 @@ struct FwdOp {
 // --------------------------------------------------------- weight gradient
 // Rows m = K index, columns n = output channel, reduction r = output pixel.
 // One CTA per (tile, KC block of pixels): it writes that block's partial to
-// the workspace, and wgrad_reduce adds the blocks in increasing order.
+// the workspace, and wgrad_reduce adds the blocks in increasing order.  The
+// gather of x is the forward's with the roles swapped: the tap part comes from
+// the row, the pixel part from the reduction-index table.
 struct WgradOp {
     ConvGeom g;
     int nchw;
     const float *dy, *x;
     float *ws;   // [nblocks][K][kn]
-    FastDiv dwo, dho, dkw, dkh, dhw;
+    FastDiv dwo, dho, dkw, dkh;
 
     __host__ __device__ int M() const { return g.K; }
     __host__ __device__ int N() const { return g.kn; }
 
-    struct Row { int valid, c, offx, offy; };
+    struct Row { int delta, ox, oy; };
     __device__ Row row(int m) const {
+        uint32_t q, ky, kx, c;
+        dkw.divmod(m < g.K ? m : 0, q, ky);
+        dkh.divmod(q, c, kx);
         Row rw;
-        rw.valid = m < g.K;
-        uint32_t t, ky, kx, c;
-        dkw.divmod(rw.valid ? m : 0, t, ky);
-        dkh.divmod(t, c, kx);
-        rw.c = c;
-        rw.offx = kx * g.vdil;
-        rw.offy = ky * g.hdil;
+        const int offx = (int) kx * g.vdil;
+        rw.oy = (int) ky * g.hdil;
+        rw.delta = nchw ? ((int) c * g.h + offx) * g.w + rw.oy : (offx * g.w + rw.oy) * g.c + (int) c;
+        rw.ox = m < g.K ? offx : -OUT;
         return rw;
     }
-    struct Col { int valid, n; };
-    __device__ Col col(int n) const { return Col{n < g.kn, n}; }
-    struct RI { int valid, bb, bix, biy, q, r; };
-    __device__ RI rinfo(int r, int rend) const {
-        RI ri;
-        ri.valid = r < rend;
-        ri.r = r;
+    struct Col { long long base; int valid; };
+    __device__ Col col(int n) const {
+        return Col{nchw ? (long long) n * g.ho * g.wo : (long long) n, n < g.kn};
+    }
+    struct alignas(16) REnt { long long base; int ix, iy; long long bd; long long pad; };
+    __device__ REnt rent(int r, int rend) const {
         uint32_t q, oy, ox, bb;
-        dwo.divmod(ri.valid ? r : 0, q, oy);
+        dwo.divmod(r < rend ? r : 0, q, oy);
         dho.divmod(q, bb, ox);
-        ri.bb = bb;
-        ri.q = ox * g.wo + oy;
-        ri.bix = ox * g.vstr - g.vpad;
-        ri.biy = oy * g.hstr - g.hpad;
-        return ri;
+        REnt t;
+        const int bix = (int) ox * g.vstr - g.vpad, biy = (int) oy * g.hstr - g.hpad;
+        t.base = nchw ? ((long long) bb * g.c * g.h + bix) * g.w + biy
+                      : (((long long) bb * g.h + bix) * g.w + biy) * g.c;
+        t.ix = r < rend ? bix : -OUT;
+        t.iy = biy;
+        const long long hw = (long long) g.ho * g.wo;
+        t.bd = r < rend ? (nchw ? (long long) bb * g.kn * hw + ((long long) ox * g.wo + oy) : (long long) r * g.kn)
+                        : -1;
+        t.pad = 0;
+        return t;
     }
-    __device__ float a(const Row &rw, const RI &ri) const {
-        int ix = ri.bix + rw.offx, iy = ri.biy + rw.offy;
-        if (!(rw.valid && ri.valid && in_range(ix, g.h) && in_range(iy, g.w))) return 0.0f;
-        size_t o = nchw ? ((((size_t) ri.bb * g.c + rw.c) * g.h + ix) * g.w + iy)
-                        : ((((size_t) ri.bb * g.h + ix) * g.w + iy) * g.c + rw.c);
-        return __ldg(x + o);
+    __device__ float a(const Row &rw, const REnt &t) const {
+        return in_range(t.ix + rw.ox, g.h) && in_range(t.iy + rw.oy, g.w) ? __ldg(x + (t.base + rw.delta)) : 0.0f;
     }
-    __device__ float b(const Col &cl, const RI &ri) const {
-        if (!(cl.valid && ri.valid)) return 0.0f;
-        size_t o = nchw ? (((size_t) ri.bb * g.kn + cl.n) * ((size_t) g.ho * g.wo) + ri.q)
-                        : ((size_t) ri.r * g.kn + cl.n);
-        return __ldg(dy + o);
+    __device__ float b(const Col &cl, const REnt &t) const {
+        return cl.valid && t.bd >= 0 ? __ldg(dy + (cl.base + t.bd)) : 0.0f;
     }
     __device__ void range(int z, int &rbeg, int &rend) const {
         rbeg = z * KC;
@@ -215,9 +230,15 @@ struct WgradOp {
 // stride below ho (same for iy).  Each (tap, KC block of l) partial is added
 // to the running value in a fixed order; the reference adds the same partials
 // with `omp atomic` in thread order (src/im2row_nhwc.c:252).
+//
+// With ih + vpad = vstr*xd + xm and kx*vdil = vstr*exd + exm (0 <= xm, exm < vstr),
+// the tap reads output row xd - exd exactly when xm == exm, so the table holds
+// (exd, exm) per r and the rows hold (xd, xm): no division per element.
 struct DgradOp {
     ConvGeom g;
-    int nchw, accumulate;
+    int nchw, accumulate;   // layout of dx; dx += result
+    int yl;                 // layout of the dy the kernel reads (0 NHWC, 1 NCHW)
+    int wl;                 // layout of w: 0 NHWC [c][tap][kn], 1 NCHW [kn][c][tap], 2 packed [tap][kn][c]
     const float *w, *dy;
     float *dx;
     FastDiv dw_, dh_, dkn, dkw, dvs, dhs;
@@ -226,50 +247,58 @@ struct DgradOp {
     __host__ __device__ int M() const { return g.b * g.h * g.w; }
     __host__ __device__ int N() const { return g.c; }
 
-    struct Row { int valid, bb, tx0, ty0; };
+    struct Row { long long base; int ix, iy, cls; };
     __device__ Row row(int m) const {
-        Row rw;
-        rw.valid = m < g.b * g.h * g.w;
-        uint32_t q, iw, ih, bb;
-        dw_.divmod(rw.valid ? m : 0, q, iw);
+        const bool valid = m < M();
+        uint32_t q, iw, ih, bb, xd, xm, yd, ym;
+        dw_.divmod(valid ? m : 0, q, iw);
         dh_.divmod(q, bb, ih);
-        rw.bb = bb;
-        rw.tx0 = ih + g.vpad;
-        rw.ty0 = iw + g.hpad;
+        dvs.divmod(ih + g.vpad, xd, xm);
+        dhs.divmod(iw + g.hpad, yd, ym);
+        Row rw;
+        rw.base = yl ? ((long long) bb * g.kn * g.ho + xd) * g.wo + yd
+                     : (((long long) bb * g.ho + xd) * g.wo + yd) * g.kn;
+        rw.ix = valid ? (int) xd : -OUT;
+        rw.iy = (int) yd;
+        rw.cls = (int) (xm | (ym << 16));
         return rw;
     }
-    struct Col { int valid, n; };
-    __device__ Col col(int n) const { return Col{n < g.c, n}; }
-    struct RI { int valid, l, kx, ky; };
-    __device__ RI rinfo(int r, int rend) const {
-        RI ri;
-        ri.valid = r < rend;
-        uint32_t tap, l, kx, ky;
-        dkn.divmod(ri.valid ? r : 0, tap, l);
+    // Single-tap NHWC: the row's reduction indices are its output pixel's channels, contiguous.
+    __device__ bool row_in(const Row &rw) const {
+        return rw.cls == 0 && in_range(rw.ix, g.ho) && in_range(rw.iy, g.wo);
+    }
+    __device__ const float *asrc() const { return dy; }
+    struct Col { long long base; int valid; };
+    __device__ Col col(int n) const {
+        const long long b = wl == 2 ? n : wl == 1 ? (long long) n * g.kh * g.kw : (long long) n * g.kh * g.kw * g.kn;
+        return Col{b, n < g.c};
+    }
+    struct alignas(16) REnt { int delta, ox, oy, cls, bd, pad0, pad1, pad2; };
+    __device__ REnt rent(int r, int rend) const {
+        uint32_t tap, l, kx, ky, exd, exm, eyd, eym;
+        dkn.divmod(r < rend ? r : 0, tap, l);
         dkw.divmod(tap, kx, ky);
-        ri.l = l;
-        ri.kx = kx;
-        ri.ky = ky;
-        return ri;
+        dvs.divmod(kx * g.vdil, exd, exm);
+        dhs.divmod(ky * g.hdil, eyd, eym);
+        REnt t;
+        t.delta = yl ? ((int) l * g.ho - (int) exd) * g.wo - (int) eyd
+                     : (int) l - ((int) exd * g.wo + (int) eyd) * g.kn;
+        t.ox = r < rend ? -(int) exd : -OUT;
+        t.oy = -(int) eyd;
+        t.cls = (int) (exm | (eym << 16));
+        t.bd = r < rend ? (wl == 2 ? r * g.c : wl == 1 ? (int) l * g.K + (int) tap : r) : -1;
+        t.pad0 = t.pad1 = t.pad2 = 0;
+        return t;
     }
-    __device__ float a(const Row &rw, const RI &ri) const {
-        int tx = rw.tx0 - ri.kx * g.vdil, ty = rw.ty0 - ri.ky * g.hdil;
-        if (!(rw.valid && ri.valid) || tx < 0 || ty < 0) return 0.0f;
-        uint32_t ox, rx, oy, ry;
-        dvs.divmod(tx, ox, rx);
-        dhs.divmod(ty, oy, ry);
-        if (rx || ry || (int) ox >= g.ho || (int) oy >= g.wo) return 0.0f;
-        size_t o = nchw ? ((((size_t) rw.bb * g.kn + ri.l) * g.ho + ox) * g.wo + oy)
-                        : ((((size_t) rw.bb * g.ho + ox) * g.wo + oy) * g.kn + ri.l);
-        return __ldg(dy + o);
+    __device__ float a(const Row &rw, const REnt &t) const {
+        return rw.cls == t.cls && in_range(rw.ix + t.ox, g.ho) && in_range(rw.iy + t.oy, g.wo)
+                   ? __ldg(dy + (rw.base + t.delta)) : 0.0f;
     }
-    __device__ float b(const Col &cl, const RI &ri) const {
-        if (!(cl.valid && ri.valid)) return 0.0f;
-        size_t k = ((size_t) cl.n * g.kh + ri.kx) * g.kw + ri.ky;
-        size_t o = nchw ? ((size_t) ri.l * g.K + k) : (k * g.kn + ri.l);
-        return __ldg(w + o);
+    __device__ float b(const Col &cl, const REnt &t) const {
+        return cl.valid && t.bd >= 0 ? __ldg(w + (cl.base + t.bd)) : 0.0f;
     }
     __host__ __device__ int segments() const { return g.kh * g.kw * ((g.kn + KC - 1) / KC); }
+    __host__ __device__ long long rlen() const { return (long long) g.kh * g.kw * g.kn; }
     __device__ void range(int z, int &rbeg, int &rend) const {
         if (ws) {
             const int nch = (g.kn + KC - 1) / KC, tap = z / nch, j = z - tap * nch;
@@ -312,29 +341,58 @@ struct DgradOp {
 };
 
 
-template <class Op>
-__global__ void __launch_bounds__(NT) fp32_igemm_kernel(const Op op) {
-    __shared__ __align__(16) float As[2][BK][BM];
-    __shared__ __align__(16) float Bs[2][BK][BN];
+// Tiles of BM x BN outputs per 256-thread CTA, 8 x 8 per thread: 128 x 128, or
+// 256 x 64 for operations with at most 64 columns (no padding columns computed).
+template <int BM_, int BN_>
+struct Tile {
+    static constexpr int BM = BM_, BN = BN_;
+    static constexpr int TX = BN / 8;                      // compute threads along n
+    static_assert((BM / 8) * (BN / 8) == NT, "8 x 8 outputs per thread");
+    static constexpr int AP = BM * BK / NT, AS = NT / BM;  // A elements per thread per slice, their r stride
+    static constexpr int BP = BN * BK / NT, BS = NT / BN;
+};
+using TileSquare = Tile<128, 128>;
+using TileTall = Tile<256, 64>;
+
+// VEC (single-tap NHWC operations): the reduction indices of an A row are consecutive
+// channels of one pixel, so each thread loads whole 4-index quads of its row as 16-byte
+// vectors (two threads cover the 8 indices of a row in a slice) instead of gathering
+// element by element down a column.
+template <class Op, class T, bool VEC>
+__global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
+    __shared__ __align__(16) float As[2][BK][T::BM];
+    __shared__ __align__(16) float Bs[2][BK][T::BN];
+    // Reduction-index table: the r part of every gather, for two chunks of NT
+    // consecutive r; chunk c + 1 is filled while the slices of chunk c run.
+    __shared__ typename Op::REnt Rt[2][NT];
     extern __shared__ float Ssm[];  // [SREGS][NT], running sum of completed KC blocks
+    constexpr int SLICES = NT / BK;  // slices per table chunk
 
     const int tid = threadIdx.x;
-    const int m0 = blockIdx.x * BM;
-    const int n0 = blockIdx.y * BN;
+    const int m0 = blockIdx.x * T::BM;
+    const int n0 = blockIdx.y * T::BN;
     const int z = blockIdx.z;
     int rbeg, rend;
     op.range(z, rbeg, rend);
+    Rt[0][tid] = op.rent(rbeg + tid, rend);
+    Rt[1][tid] = op.rent(rbeg + NT + tid, rend);
 
-    // loader mapping: element (lk + 2i, lm) of each 8x128 slice
-    const int lm = tid & 127, lk = tid >> 7;
-    const auto arow = op.row(m0 + lm);
-    const auto bcol = op.col(n0 + lm);
-    float ra[4], rb[4];
+    // loader mapping: A element (ak + AS*i, am), B element (bk + BS*i, bn) of each slice;
+    // VEC: A quads vq .. vq + VQ - 1 (indices 4*vq ...) of row am
+    constexpr int TPR = NT / T::BM, VQ = (BK / 4) / TPR;
+    static_assert(!VEC || 4 * VQ == T::AP, "a thread's A quads cover its A elements");
+    const int am = VEC ? tid / TPR : tid % T::BM, ak = tid / T::BM, vq = (tid % TPR) * VQ;
+    const int bn = tid % T::BN, bk = tid / T::BN;
+    const auto arow = op.row(m0 + am);
+    const auto bcol = op.col(n0 + bn);
+    float ra[T::AP], rb[T::BP];
+    const float *vsrc = nullptr;
+    if constexpr (VEC) vsrc = op.row_in(arow) ? op.asrc() + arow.base : nullptr;
 
-    // compute mapping: rows {ty*4+i, 64+ty*4+i}, columns {tx*4+j, 64+tx*4+j}
-    const int tx = tid & 15, ty = tid >> 4;
-    auto mrow = [&](int i) { return m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4); };
-    auto ncol = [&](int j) { return n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4); };
+    // compute mapping: rows {ty*4+i, BM/2+ty*4+i}, columns {tx*4+j, BN/2+tx*4+j}
+    const int tx = tid % T::TX, ty = tid / T::TX;
+    auto mrow = [&](int i) { return m0 + (i < 4 ? ty * 4 + i : T::BM / 2 + ty * 4 + i - 4); };
+    auto ncol = [&](int j) { return n0 + (j < 4 ? tx * 4 + j : T::BN / 2 + tx * 4 + j - 4); };
 
 #pragma unroll
     for (int i = 0; i < 8; i++)
@@ -358,47 +416,89 @@ __global__ void __launch_bounds__(NT) fp32_igemm_kernel(const Op op) {
             }
     };
 
-    auto gload = [&](int r0) {
+    auto gload = [&](int t) {
+        const int rr = t * BK;   // slices never straddle a chunk: NT % BK == 0
+        const typename Op::REnt *rt = Rt[(rr / NT) & 1] + rr % NT;
+        if constexpr (VEC) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const auto ri = op.rinfo(r0 + lk + 2 * i, rend);
-            ra[i] = op.a(arow, ri);
-            rb[i] = op.b(bcol, ri);
+            for (int q = 0; q < VQ; q++) {
+                const int r = rbeg + rr + 4 * (vq + q);
+                float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (vsrc) {
+                    if (r + 3 < rend) {
+                        v = __ldg(reinterpret_cast<const float4 *>(vsrc + r));
+                    } else {
+                        if (r < rend) v.x = __ldg(vsrc + r);
+                        if (r + 1 < rend) v.y = __ldg(vsrc + r + 1);
+                        if (r + 2 < rend) v.z = __ldg(vsrc + r + 2);
+                    }
+                }
+                ra[4 * q] = v.x;
+                ra[4 * q + 1] = v.y;
+                ra[4 * q + 2] = v.z;
+                ra[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < T::AP; i++) ra[i] = op.a(arow, rt[ak + T::AS * i]);
         }
+#pragma unroll
+        for (int i = 0; i < T::BP; i++) rb[i] = op.b(bcol, rt[bk + T::BS * i]);
     };
     auto sstore = [&](int buf) {
+        if constexpr (VEC) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            As[buf][lk + 2 * i][lm] = ra[i];
-            Bs[buf][lk + 2 * i][lm] = rb[i];
+            for (int q = 0; q < VQ; q++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) As[buf][4 * (vq + q) + j][am] = ra[4 * q + j];
+        } else {
+#pragma unroll
+            for (int i = 0; i < T::AP; i++) As[buf][ak + T::AS * i][am] = ra[i];
         }
+#pragma unroll
+        for (int i = 0; i < T::BP; i++) Bs[buf][bk + T::BS * i][bn] = rb[i];
+    };
+    auto step = [&](int buf, int kk) {
+        const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][T::BM / 2 + ty * 4]);
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][T::BN / 2 + tx * 4]);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
     };
 
     const int ntiles = (rend - rbeg + BK - 1) / BK;
     int next_fold = op.next_fold(rbeg, rend);
-    gload(rbeg);
+    __syncthreads();
+    gload(0);
     sstore(0);
     __syncthreads();
     for (int t = 0; t < ntiles; t++) {
         const int buf = t & 1;
-        if (t + 1 < ntiles) gload(rbeg + (t + 1) * BK);
+        if (t > 0 && t % SLICES == 0) {
+            // chunk c + 1 replaces chunk c - 1, whose last reader (slice 32c - 1's
+            // loads, issued during slice 32c - 2) is behind two barriers
+            const int c = t / SLICES + 1;
+            Rt[c & 1][tid] = op.rent(rbeg + c * NT + tid, rend);
+        }
+        if (t + 1 < ntiles) gload(t + 1);
+        const int r0 = rbeg + t * BK;
+        if (next_fold >= r0 + BK) {
 #pragma unroll
-        for (int kk = 0; kk < BK; kk++) {
-            const int r = rbeg + t * BK + kk;
-            if (r == next_fold) {
-                fold();
-                next_fold = op.next_fold(r, rend);
+            for (int kk = 0; kk < BK; kk++) step(buf, kk);
+        } else {
+#pragma unroll 1
+            for (int kk = 0; kk < BK; kk++) {
+                if (r0 + kk == next_fold) {
+                    fold();
+                    next_fold = op.next_fold(r0 + kk, rend);
+                }
+                step(buf, kk);
             }
-            const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
-            const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][64 + ty * 4]);
-            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
-            const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][64 + tx * 4]);
-            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-#pragma unroll
-            for (int i = 0; i < 8; i++)
-#pragma unroll
-                for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
         }
         if (t + 1 < ntiles) sstore(buf ^ 1);
         __syncthreads();
@@ -460,42 +560,69 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <class Op>
-cudaError_t launch(const Op &op, int gz, cudaStream_t st) {
+template <class Op, class T, bool VEC>
+cudaError_t launch_tile(const Op &op, int gz, cudaStream_t st) {
     static bool attr_set = false;  // per template instance; harmless if set twice
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(fp32_igemm_kernel<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int) S_SMEM_BYTES);
+        cudaError_t e = cudaFuncSetAttribute(fp32_igemm_kernel<Op, T, VEC>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int) S_SMEM_BYTES);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    dim3 grid((op.M() + BM - 1) / BM, (op.N() + BN - 1) / BN, gz);
+    dim3 grid((op.M() + T::BM - 1) / T::BM, (op.N() + T::BN - 1) / T::BN, gz);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    fp32_igemm_kernel<Op><<<grid, NT, S_SMEM_BYTES, st>>>(op); cg_note_launch();
+    fp32_igemm_kernel<Op, T, VEC><<<grid, NT, S_SMEM_BYTES, st>>>(op); cg_note_launch();
     return cudaGetLastError();
 }
 
-// Scratch planes of the block split, one grow-only buffer per (device, stream): a CUDA graph
-// that captured a buffer keeps using it, so buffers are never freed or reused for another stream.
-std::mutex g_split_mu;
-std::map<std::pair<int, cudaStream_t>, std::pair<float *, size_t>> g_split_ws;
-constexpr size_t SPLIT_WS_MAX = (size_t) 256 << 20;
+// 256 x 64 tiles where a 128-wide tile would compute padding columns.
+inline bool tall_tiles(int N) { return N <= 64; }
 
-float *split_scratch(size_t bytes, cudaStream_t st) {
-    if (bytes > SPLIT_WS_MAX) return nullptr;
+template <class Op, bool VEC>
+cudaError_t launch_shape(const Op &op, int gz, cudaStream_t st) {
+    return tall_tiles(op.N()) ? launch_tile<Op, TileTall, VEC>(op, gz, st)
+                              : launch_tile<Op, TileSquare, VEC>(op, gz, st);
+}
+
+template <class Op>
+cudaError_t launch(const Op &op, int gz, bool vec, cudaStream_t st) {
+    if constexpr (!std::is_same<Op, WgradOp>::value) {
+        if (vec) return launch_shape<Op, true>(op, gz, st);
+    }
+    return launch_shape<Op, false>(op, gz, st);
+}
+
+// Gathers add 32-bit offsets within one image and within the weights.
+inline bool offsets_fit(const ConvGeom &g) {
+    const long long lim = INT_MAX / 2;
+    return (long long) g.c * g.h * g.w < lim && (long long) g.kn * g.ho * g.wo < lim &&
+           (long long) g.K * g.kn < lim;
+}
+
+// Library-owned scratch, one grow-only buffer per (device, stream, purpose): a CUDA graph
+// that captured a buffer keeps using it, so buffers are never freed or reused for another
+// stream.  Purposes: the block split's planes, an operand copy in the kernel's gather layout
+// (activation), a repacked weight tensor.
+enum { SLOT_SPLIT = 0, SLOT_ACT = 1, SLOT_WGT = 2 };
+constexpr size_t SLOT_MAX[3] = {(size_t) 256 << 20, (size_t) 4 << 30, (size_t) 256 << 20};
+std::mutex g_scratch_mu;
+std::map<std::tuple<int, cudaStream_t, int>, std::pair<float *, size_t>> g_scratch;
+
+float *scratch(int slot, size_t bytes, cudaStream_t st) {
+    if (bytes == 0 || bytes > SLOT_MAX[slot]) return nullptr;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    std::lock_guard<std::mutex> lk(g_split_mu);
-    auto &e = g_split_ws[{dev, st}];
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    auto &e = g_scratch[std::make_tuple(dev, st, slot)];
     if (e.second >= bytes) return e.first;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
         cudaGetLastError();
-        return nullptr;   // no allocation under capture: the fused form runs instead
+        return nullptr;   // no allocation under capture: the form without scratch runs instead
     }
     size_t want = e.second ? e.second : ((size_t) 32 << 20);
     while (want < bytes) want *= 2;
-    if (want > SPLIT_WS_MAX) want = SPLIT_WS_MAX;
+    if (want > SLOT_MAX[slot]) want = SLOT_MAX[slot];
     float *p = nullptr;
     if (cudaMalloc(&p, want) != cudaSuccess) {
         cudaGetLastError();
@@ -505,21 +632,62 @@ float *split_scratch(size_t bytes, cudaStream_t st) {
     return p;
 }
 
-// The block split pays when the fused grid leaves SMs idle (two 128x128 CTAs fit per SM).
+// dst[b][c][r] = src[b][r][c] through 32 x 33 shared-memory tiles (both sides coalesced).
+__global__ void transpose_kernel(const float *__restrict__ src, float *__restrict__ dst, int R, int C) {
+    __shared__ float t[32][33];
+    const size_t off = (size_t) blockIdx.z * R * C;
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += 8) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < R && c < C) t[i][threadIdx.x] = src[off + (size_t) r * C + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < R && c < C) dst[off + (size_t) c * R + r] = t[threadIdx.x][i];
+    }
+}
+
+// A transposed copy of src ([batch][R][C] -> [batch][C][R]) in the given scratch slot, or NULL
+// when there is no room (or the grid would not fit); the caller then reads src as it is.
+const float *transposed(int slot, const float *src, long long batch, long long R, long long C, cudaStream_t st) {
+    const long long gy = (R + 31) / 32, gx = (C + 31) / 32;
+    if (batch < 1 || batch > 65535 || gy > 65535 || gx > INT_MAX) return nullptr;
+    float *dst = scratch(slot, sizeof(float) * (size_t) (batch * R * C), st);
+    if (!dst) return nullptr;
+    transpose_kernel<<<dim3((unsigned) gx, (unsigned) gy, (unsigned) batch), dim3(32, 8), 0, st>>>(src, dst, (int) R,
+                                                                                                   (int) C);
+    cg_note_launch();
+    if (cudaGetLastError() != cudaSuccess) return nullptr;
+    return dst;
+}
+
+inline bool aligned16(const void *p) { return ((uintptr_t) p & 15) == 0; }
+
+// The block split pays when the fused grid leaves SMs idle or ends in a thin last wave (two
+// CTAs fit per SM), weighed against the planes it writes and reads back.  Model: the kernel's
+// rate at full waves (about 35 TFLOP/s) scaled by the fraction of CTA slots its waves fill,
+// plus the planes' bytes at about 4 TB/s.
 template <class Op>
-cudaError_t launch_split_or_fused(Op op, int M, int N, cudaStream_t st) {
-    const long long tiles = (long long) ((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, cudaStream_t st) {
+    const int bm = tall_tiles(N) ? TileTall::BM : TileSquare::BM, bn = tall_tiles(N) ? TileTall::BN : TileSquare::BN;
+    const long long tiles = (long long) ((M + bm - 1) / bm) * ((N + bn - 1) / bn);
     const int nz = op.segments();
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     op.ws = nullptr;
-    if (nz > 1 && tiles < 2LL * sms) {
+    if (nz > 1 && tiles > 0) {
+        const double slots = 2.0 * sms;
+        auto filled = [&](double n) { return n / (std::ceil(n / slots) * slots); };
         const size_t bytes = sizeof(float) * (size_t) nz * (size_t) M * (size_t) N;
-        op.ws = split_scratch(bytes, st);
+        const double flops = 2.0 * M * N * (double) op.rlen(), rate = 35e12;
+        const double t_fused = flops / (rate * filled((double) tiles));
+        const double t_split = flops / (rate * filled((double) tiles * nz)) + 2.0 * (double) bytes / 4e12;
+        if (t_split < t_fused) op.ws = scratch(SLOT_SPLIT, bytes, st);
     }
-    if (!op.ws) return launch(op, 1, st);
-    cudaError_t e = launch(op, nz, st);
+    if (!op.ws) return launch(op, 1, vec, st);
+    cudaError_t e = launch(op, nz, vec, st);
     if (e != cudaSuccess) return e;
     const long long total = (long long) M * N;
     const int blocks = (int) std::min<long long>((total + 255) / 256, (long long) sms * 16);
@@ -530,11 +698,18 @@ cudaError_t launch_split_or_fused(Op op, int M, int N, cudaStream_t st) {
 
 }  // namespace
 
+// Operand layouts the kernel reads (the arithmetic and its order do not depend on them):
+// a k x k NHWC forward reads x from an NCHW copy (a column of A, 128 output pixels at one
+// reduction index, is then 128 consecutive floats instead of 128 pixels c floats apart);
+// a single-tap NHWC forward reads x rows as 16-byte channel vectors; an NCHW forward reads
+// its weights as [K][kn] (a row of B contiguous).
 cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float *x, float *y,
                         const cg_epi &e, cudaStream_t st) {
     FwdOp op;
     op.g = make_geom(s);
+    if (!offsets_fit(op.g)) return cudaErrorNotSupported;
     op.nchw = nchw;
+    op.xl = op.wl = nchw;
     op.w = w;
     op.x = x;
     op.y = y;
@@ -544,7 +719,19 @@ cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float
     op.dkw = FastDiv(s.kw);
     op.dkh = FastDiv(s.kh);
     op.ws = nullptr;
-    return launch_split_or_fused(op, (int) op.g.P, op.g.kn, st);
+    bool vec = false;
+    if (!nchw) {
+        if (s.kh == 1 && s.kw == 1) {
+            vec = s.c % 4 == 0 && aligned16(x);
+        } else if (const float *xt = transposed(SLOT_ACT, x, s.b, (long long) s.h * s.w, s.c, st)) {
+            op.x = xt;
+            op.xl = 1;
+        }
+    } else if (const float *wt = transposed(SLOT_WGT, w, 1, s.kn, op.g.K, st)) {
+        op.w = wt;
+        op.wl = 0;
+    }
+    return launch_split_or_fused(op, (int) op.g.P, op.g.kn, vec, st);
 }
 
 size_t cg_fp32_wgrad_ws_bytes(const cg_shape &s) {
@@ -557,6 +744,7 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
                           cudaStream_t st) {
     WgradOp op;
     op.g = make_geom(s);
+    if (!offsets_fit(op.g)) return cudaErrorNotSupported;
     op.nchw = nchw;
     op.dy = dy;
     op.x = x;
@@ -565,9 +753,8 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     op.dho = FastDiv(op.g.ho);
     op.dkw = FastDiv(s.kw);
     op.dkh = FastDiv(s.kh);
-    op.dhw = FastDiv(op.g.ho * op.g.wo);
     const int nblocks = (int) ((op.g.P + KC - 1) / KC);
-    cudaError_t e = launch(op, nblocks, st);
+    cudaError_t e = launch(op, nblocks, false, st);
     if (e != cudaSuccess) return e;
     const long long total = (long long) op.g.K * op.g.kn;
     int blocks = (int) std::min<long long>((total + 255) / 256, 152LL * 16);
@@ -575,12 +762,17 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     return cudaGetLastError();
 }
 
+// Operand layouts as in the forward: a k x k NHWC input gradient reads dy from an NCHW copy,
+// a single-tap NHWC one reads dy rows as channel vectors, and the weights are read as
+// [tap][kn][c] (a row of B, consecutive input channels at one (tap, output channel), contiguous).
 cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const float *dy, float *dx, int accumulate,
                           cudaStream_t st) {
     DgradOp op;
     op.g = make_geom(s);
+    if (!offsets_fit(op.g)) return cudaErrorNotSupported;
     op.nchw = nchw;
     op.accumulate = accumulate;
+    op.yl = op.wl = nchw;
     op.w = w;
     op.dy = dy;
     op.dx = dx;
@@ -591,5 +783,25 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     op.dvs = FastDiv(s.vstride);
     op.dhs = FastDiv(s.hstride);
     op.ws = nullptr;
-    return launch_split_or_fused(op, op.M(), op.g.c, st);
+    const int taps = s.kh * s.kw;
+    bool vec = false;
+    if (!nchw) {
+        if (taps == 1) {
+            vec = s.kn % 4 == 0 && aligned16(dy);
+        } else if (const float *t = transposed(SLOT_ACT, dy, s.b, (long long) op.g.ho * op.g.wo, s.kn, st)) {
+            op.dy = t;
+            op.yl = 1;
+        }
+    }
+    // NHWC w is [c][tap*kn], NCHW w is [kn*c][tap]; both transpose to [tap][kn][c]
+    const float *wt = nullptr;
+    if (!nchw) wt = transposed(SLOT_WGT, w, 1, s.c, (long long) taps * s.kn, st);
+    else if (taps > 1) wt = transposed(SLOT_WGT, w, 1, (long long) s.kn * s.c, taps, st);
+    if (wt) {
+        op.w = wt;
+        op.wl = 2;
+    } else if (nchw && taps == 1) {
+        op.wl = 2;   // [kn][c] is [tap][kn][c] already
+    }
+    return launch_split_or_fused(op, op.M(), op.g.c, vec, st);
 }

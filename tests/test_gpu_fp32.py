@@ -127,14 +127,18 @@ def test_random_shapes_against_restatement(cglib, oracle_lib, seed):
 
 
 @pytest.mark.parametrize("b,h,w,c,kn", [
-    (2, 7, 7, 512, 512),     # 4 tiles: one CTA per (tile, KC block), 12 blocks, ordered reduction
-    (4, 56, 56, 64, 512),    # 392 tiles: the fused form, 2 KC blocks folded in the kernel
+    (2, 7, 7, 512, 512),     # 4 tiles: one CTA per (tile, KC block) in both operations, ordered reduction
+    (4, 64, 76, 64, 512),    # forward: 608 tiles (4 full waves on 152 SMs), fused, 2 KC blocks folded;
+                             # input gradient: 76 tiles of 256 x 64, split into 18 segments
+    (8, 64, 76, 128, 64),    # forward: 152 tiles of 256 x 64, split into 3 KC blocks;
+                             # input gradient: 304 tiles (one full wave), fused, 9 taps folded
 ])
 def test_block_split_and_fused_forms_follow_reference_order(cglib, oracle_lib, b, h, w, c, kn):
-    """Small grids run the forward and input gradient one CTA per reduction segment and add the
-    segments in order in a second kernel; large grids fold them inside one kernel.  The forward
-    keeps the reference's bits in both forms (both layouts, with the epilogue); the input gradient,
-    plain and accumulating, stays within FP32 tolerance of the port."""
+    """Grids that leave SMs idle or end in a thin last wave run the forward and input gradient one
+    CTA per reduction segment and add the segments in order in a second kernel; grids of full
+    waves fold them inside one kernel.  The forward keeps the reference's bits in both forms (both
+    layouts, with the epilogue); the input gradient, plain and accumulating, stays within FP32
+    tolerance of the port and is reproducible."""
     g = C.geom(b, h, w, c, kn, 3, 3, pad=1)
     rng = np.random.default_rng(b * 1000 + kn)
     K = 9 * c
