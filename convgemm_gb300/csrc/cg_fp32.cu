@@ -124,7 +124,7 @@ struct FwdOp {
     }
     __host__ __device__ int segments() const { return (g.K + KC - 1) / KC; }
     __host__ __device__ long long rlen() const { return g.K; }
-    __device__ void range(int z, int &rbeg, int &rend) const {
+    __device__ void range(int m0, int z, int &rbeg, int &rend) const {
         if (ws) {
             rbeg = z * KC;
             rend = min(g.K, rbeg + KC);
@@ -138,6 +138,8 @@ struct FwdOp {
         return nf >= rend ? INT_MAX : nf;
     }
     __device__ float s_init(int m, int n) const { return 0.0f; }
+    __device__ float s_start(int m, int n) const { return 0.0f; }
+    __device__ int zcount(int m, int nz) const { return nz; }
     __device__ void finish_z(int z, int m, int n, float s) const {
         if (!ws) return finish(m, n, s);
         if (m < (int) g.P && n < g.kn) ws[((size_t) z * g.P + m) * g.kn + n] = s;
@@ -211,7 +213,7 @@ struct WgradOp {
     __device__ float b(const Col &cl, const REnt &t) const {
         return cl.valid && t.bd >= 0 ? __ldg(dy + (cl.base + t.bd)) : 0.0f;
     }
-    __device__ void range(int z, int &rbeg, int &rend) const {
+    __device__ void range(int m0, int z, int &rbeg, int &rend) const {
         rbeg = z * KC;
         rend = min((long long) (z + 1) * KC, g.P);
     }
@@ -299,7 +301,7 @@ struct DgradOp {
     }
     __host__ __device__ int segments() const { return g.kh * g.kw * ((g.kn + KC - 1) / KC); }
     __host__ __device__ long long rlen() const { return (long long) g.kh * g.kw * g.kn; }
-    __device__ void range(int z, int &rbeg, int &rend) const {
+    __device__ void range(int m0, int z, int &rbeg, int &rend) const {
         if (ws) {
             const int nch = (g.kn + KC - 1) / KC, tap = z / nch, j = z - tap * nch;
             rbeg = tap * g.kn + j * KC;
@@ -330,6 +332,7 @@ struct DgradOp {
         if (!accumulate || m >= M() || n >= g.c) return 0.0f;
         return dx[out_index(m, n)];
     }
+    __device__ int zcount(int m, int nz) const { return nz; }
     __device__ void finish_z(int z, int m, int n, float s) const {
         if (!ws) return finish(m, n, s);
         if (m < M() && n < g.c) ws[((size_t) z * M() + m) * g.c + n] = s;
@@ -340,6 +343,150 @@ struct DgradOp {
     }
 };
 
+
+// ------------------------------------------- input gradient, strided layers
+// The gather form above runs every tap for every input pixel, although with strides
+// (sv, sh) a pixel of stride phase (xm, ym) = ((ih + vpad) % sv, (iw + hpad) % sh) is
+// reached only by the taps of the same phase.  Here the GEMM rows are the input pixels
+// grouped by phase (each phase padded to a multiple of 256 rows, so no tile straddles
+// two), and a phase's reduction runs over its own taps only, in increasing tap order:
+// the segments (tap, KC block of kn) of a pixel are those of the gather form minus the
+// ones whose products are all zero, added in the same order.
+constexpr int DG_MAXCLS = 16, DG_MAXTAPS = 64;
+struct DgPhase {
+    int mbeg, rows;   // first (padded) GEMM row, pixels of this phase
+    int ih0, iw0;     // first input row / column of this phase
+    int rbeg, ntaps;  // reduction indices [rbeg, rbeg + ntaps*kn), taps tap0 .. tap0 + ntaps - 1
+    int tap0;
+    FastDiv dwc, dhc; // phase columns and rows per image
+};
+struct DgradPhaseOp {
+    ConvGeom g;
+    int nchw, accumulate, yl, wl;   // as in DgradOp
+    const float *w, *dy;
+    float *dx;
+    FastDiv dkn, dvs, dhs;
+    int ncls, mpad, nkb;            // phases, padded rows, KC blocks per tap
+    DgPhase ph[DG_MAXCLS];
+    unsigned char taps[DG_MAXTAPS]; // tap indices kx*kw + ky grouped by phase
+    float *ws;
+
+    __host__ __device__ int M() const { return mpad; }
+    __host__ __device__ int N() const { return g.c; }
+    __device__ int phase_of_m(int m) const {
+        int c = 0;
+        for (int i = 1; i < ncls; i++) c = m >= ph[i].mbeg ? i : c;
+        return c;
+    }
+    __device__ int phase_of_r(int r) const {
+        int c = 0;
+        for (int i = 1; i < ncls; i++) c = r >= ph[i].rbeg && ph[i].ntaps ? i : c;
+        return c;
+    }
+    // GEMM row -> input pixel (b, ih, iw), or false for padding rows
+    __device__ bool pixel(int m, uint32_t &bb, int &ih, int &iw) const {
+        const DgPhase &p = ph[phase_of_m(m)];
+        const int loc = m - p.mbeg;
+        uint32_t q, tw, th;
+        p.dwc.divmod(loc < p.rows ? loc : 0, q, tw);
+        p.dhc.divmod(q, bb, th);
+        ih = p.ih0 + (int) th * g.vstr;
+        iw = p.iw0 + (int) tw * g.hstr;
+        return loc < p.rows;
+    }
+
+    struct Row { long long base; int ix, iy; };
+    __device__ Row row(int m) const {
+        uint32_t bb;
+        int ih, iw;
+        const bool valid = pixel(m, bb, ih, iw);
+        const int xd = (ih + g.vpad) / g.vstr, yd = (iw + g.hpad) / g.hstr;   // exact for this phase
+        Row rw;
+        rw.base = yl ? ((long long) bb * g.kn * g.ho + xd) * g.wo + yd
+                     : (((long long) bb * g.ho + xd) * g.wo + yd) * g.kn;
+        rw.ix = valid ? xd : -OUT;
+        rw.iy = yd;
+        return rw;
+    }
+    __device__ bool row_in(const Row &rw) const { return in_range(rw.ix, g.ho) && in_range(rw.iy, g.wo); }
+    __device__ const float *asrc() const { return dy; }
+    struct Col { long long base; int valid; };
+    __device__ Col col(int n) const {
+        const long long b = wl == 2 ? n : wl == 1 ? (long long) n * g.kh * g.kw : (long long) n * g.kh * g.kw * g.kn;
+        return Col{b, n < g.c};
+    }
+    struct alignas(16) REnt { int delta, ox, oy, bd; };
+    __device__ REnt rent(int r, int rend) const {
+        const DgPhase &p = ph[phase_of_r(r)];
+        uint32_t j, l;
+        dkn.divmod(r < rend ? r - p.rbeg : 0, j, l);
+        const int tap = p.ntaps > 0 ? taps[p.tap0 + min((int) j, p.ntaps - 1)] : 0;
+        const int kx = tap / g.kw, ky = tap - kx * g.kw;
+        const int exd = kx * g.vdil / g.vstr, eyd = ky * g.hdil / g.hstr;
+        REnt t;
+        t.delta = yl ? ((int) l * g.ho - exd) * g.wo - eyd : (int) l - (exd * g.wo + eyd) * g.kn;
+        t.ox = r < rend ? -exd : -OUT;
+        t.oy = -eyd;
+        const int rg = tap * g.kn + (int) l;   // reduction index of the gather form
+        t.bd = r < rend ? (wl == 2 ? rg * g.c : wl == 1 ? (int) l * g.K + tap : rg) : -1;
+        return t;
+    }
+    __device__ float a(const Row &rw, const REnt &t) const {
+        return in_range(rw.ix + t.ox, g.ho) && in_range(rw.iy + t.oy, g.wo) ? __ldg(dy + (rw.base + t.delta)) : 0.0f;
+    }
+    __device__ float b(const Col &cl, const REnt &t) const {
+        return cl.valid && t.bd >= 0 ? __ldg(w + (cl.base + t.bd)) : 0.0f;
+    }
+    __host__ __device__ int segments() const {
+        int nt = 0;
+        for (int i = 0; i < ncls; i++) nt = ph[i].ntaps > nt ? ph[i].ntaps : nt;
+        return nt * nkb;
+    }
+    __host__ __device__ long long rlen() const { return (long long) segments() * min(g.kn, KC); }
+    __device__ void range(int m0, int z, int &rbeg, int &rend) const {
+        const DgPhase &p = ph[phase_of_m(m0)];
+        if (ws) {
+            const int j = z / nkb, kb = z - j * nkb;
+            if (j >= p.ntaps) {
+                rbeg = rend = p.rbeg;
+                return;
+            }
+            rbeg = p.rbeg + j * g.kn + kb * KC;
+            rend = p.rbeg + j * g.kn + min(g.kn, (kb + 1) * KC);
+        } else {
+            rbeg = p.rbeg;
+            rend = p.rbeg + p.ntaps * g.kn;
+        }
+    }
+    __device__ int next_fold(int r, int rend) const {
+        const DgPhase &p = ph[phase_of_r(r)];
+        uint32_t j, l;
+        dkn.divmod(r - p.rbeg, j, l);
+        int nf = r - (int) l + min(g.kn, (int) (l / KC + 1) * KC);
+        return nf >= rend ? INT_MAX : nf;
+    }
+    __device__ int zcount(int m, int nz) const { return ph[phase_of_m(m)].ntaps * nkb; }
+    __device__ bool out_index(int m, int n, size_t &o) const {
+        uint32_t bb;
+        int ih, iw;
+        if (!pixel(m, bb, ih, iw) || n >= g.c) return false;
+        o = nchw ? (((size_t) bb * g.c + n) * g.h + ih) * g.w + iw : (((size_t) bb * g.h + ih) * g.w + iw) * g.c + n;
+        return true;
+    }
+    __device__ float s_start(int m, int n) const {
+        size_t o;
+        return accumulate && out_index(m, n, o) ? dx[o] : 0.0f;
+    }
+    __device__ float s_init(int m, int n) const { return ws ? 0.0f : s_start(m, n); }
+    __device__ void finish_z(int z, int m, int n, float s) const {
+        if (!ws) return finish(m, n, s);
+        if (z < zcount(m, 0) && n < g.c) ws[((size_t) z * mpad + m) * g.c + n] = s;
+    }
+    __device__ void finish(int m, int n, float s) const {
+        size_t o;
+        if (out_index(m, n, o)) dx[o] = s;
+    }
+};
 
 // Tiles of BM x BN outputs per 256-thread CTA, 8 x 8 per thread: 128 x 128, or
 // 256 x 64 for operations with at most 64 columns (no padding columns computed).
@@ -373,7 +520,7 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
     const int n0 = blockIdx.y * T::BN;
     const int z = blockIdx.z;
     int rbeg, rend;
-    op.range(z, rbeg, rend);
+    op.range(m0, z, rbeg, rend);
     Rt[0][tid] = op.rent(rbeg + tid, rend);
     Rt[1][tid] = op.rent(rbeg + NT + tid, rend);
 
@@ -503,7 +650,7 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
         if (t + 1 < ntiles) sstore(buf ^ 1);
         __syncthreads();
     }
-    fold();
+    if (ntiles > 0) fold();   // an empty range leaves the start value as it is
 
 #pragma unroll
     for (int i = 0; i < 8; i++)
@@ -522,18 +669,17 @@ __global__ void fp32_split_reduce_kernel(const Op op, const float *__restrict__ 
     for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
          i += (long long) gridDim.x * blockDim.x) {
         const int m = (int) (i / N), n = (int) (i % N);
-        float s;
-        if constexpr (std::is_same<Op, DgradOp>::value) s = op.s_start(m, n);
-        else s = 0.0f;
+        float s = op.s_start(m, n);
+        const int nzr = op.zcount(m, nz);
         int z = 0;
-        for (; z + 8 <= nz; z += 8) {
+        for (; z + 8 <= nzr; z += 8) {
             float v[8];
 #pragma unroll
             for (int j = 0; j < 8; j++) v[j] = ws[(size_t) (z + j) * total + i];
 #pragma unroll
             for (int j = 0; j < 8; j++) s = __fadd_rn(s, v[j]);
         }
-        for (; z < nz; z++) s = __fadd_rn(s, ws[(size_t) z * total + i]);
+        for (; z < nzr; z++) s = __fadd_rn(s, ws[(size_t) z * total + i]);
         op.finish(m, n, s);
     }
 }
@@ -784,6 +930,7 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     op.dhs = FastDiv(s.hstride);
     op.ws = nullptr;
     const int taps = s.kh * s.kw;
+    const bool phased = (s.vstride > 1 || s.hstride > 1) && s.vstride * s.hstride <= DG_MAXCLS && taps <= DG_MAXTAPS;
     bool vec = false;
     if (!nchw) {
         if (taps == 1) {
@@ -803,5 +950,46 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     } else if (nchw && taps == 1) {
         op.wl = 2;   // [kn][c] is [tap][kn][c] already
     }
-    return launch_split_or_fused(op, op.M(), op.g.c, vec, st);
+    if (!phased) return launch_split_or_fused(op, op.M(), op.g.c, vec, st);
+
+    DgradPhaseOp po;
+    po.g = op.g;
+    po.nchw = nchw;
+    po.accumulate = accumulate;
+    po.yl = op.yl;
+    po.wl = op.wl;
+    po.w = op.w;
+    po.dy = op.dy;
+    po.dx = dx;
+    po.dkn = FastDiv(s.kn);
+    po.nkb = (s.kn + KC - 1) / KC;
+    po.ws = nullptr;
+    long long m = 0;
+    int r = 0, t0 = 0, c = 0;
+    for (int xm = 0; xm < s.vstride; xm++)
+        for (int ym = 0; ym < s.hstride; ym++, c++) {
+            DgPhase &p = po.ph[c];
+            p.ih0 = ((xm - s.vpad) % s.vstride + s.vstride) % s.vstride;
+            p.iw0 = ((ym - s.hpad) % s.hstride + s.hstride) % s.hstride;
+            const int hc = p.ih0 < s.h ? (s.h - p.ih0 + s.vstride - 1) / s.vstride : 0;
+            const int wc = p.iw0 < s.w ? (s.w - p.iw0 + s.hstride - 1) / s.hstride : 0;
+            p.rows = s.b * hc * wc;
+            p.dhc = FastDiv(hc > 0 ? hc : 1);
+            p.dwc = FastDiv(wc > 0 ? wc : 1);
+            p.mbeg = (int) m;
+            p.rbeg = r;
+            p.tap0 = t0;
+            p.ntaps = 0;
+            for (int kx = 0; kx < s.kh; kx++)
+                for (int ky = 0; ky < s.kw; ky++)
+                    if ((kx * s.vdil) % s.vstride == xm && (ky * s.hdil) % s.hstride == ym)
+                        po.taps[t0 + p.ntaps++] = (unsigned char) (kx * s.kw + ky);
+            t0 += p.ntaps;
+            r += p.ntaps * s.kn;
+            m += ((long long) p.rows + 255) / 256 * 256;
+        }
+    if (m > INT_MAX / 2) return cudaErrorNotSupported;
+    po.ncls = c;
+    po.mpad = (int) m;
+    return launch_split_or_fused(po, po.mpad, s.c, vec && taps == 1, st);
 }
