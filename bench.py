@@ -465,10 +465,13 @@ def per_layer_table(torch, net, layers, batch, peaks, path, reps=20):
 def run_only(torch, cg, tc, layers, batch, args):
     name, op = args.only.split(":")
     idx = next(i for i, l in enumerate(layers) if l["name"] == name)
-    net = Net(torch, cg, tc, [layers[idx]], batch, with_fp32=False)
+    f32 = op.endswith("32")
+    net = Net(torch, cg, tc, [layers[idx]], batch, with_fp32=f32)
     d = net.L[0]
     d["first"] = False
     s = d["s"]
+    if f32 and d["dx32"] is None:
+        d["dx32"] = torch.empty(batch, s.h, s.w, s.c, device="cuda")
     if d["wpd"] is None:
         d["wpd"] = torch.empty(tc.weights_size(s, tc.OPERAND_DGRAD) // 2, device="cuda", dtype=torch.bfloat16)
         d["dx"] = torch.empty(batch, s.h, s.w, s.c, device="cuda", dtype=torch.bfloat16)
@@ -482,7 +485,11 @@ def run_only(torch, cg, tc, layers, batch, args):
         net.resize_workspace()
     fn = {"fwd": lambda: tc.fwd_bf16(s, d["x"], d["wp"], d["y"], d["scale"], d["shift"], relu=d["relu"]),
           "dgrad": lambda: tc.dgrad_bf16(s, d["dy"], d["wpd"], d["dx"]),
-          "wgrad": lambda: tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], net.ws)}[op]
+          "wgrad": lambda: tc.wgrad_bf16(cg.NHWC, s, d["dy"], d["x"], d["dw"], net.ws),
+          "fwd32": lambda: cg.fwd_f32(cg.NHWC, s, d["w32"], d["x32"], d["y32"], mean=d["mean"],
+                                      inv_std=d["inv_std"], gamma=d["gamma"], beta=d["beta"], relu=d["relu"]),
+          "dgrad32": lambda: cg.dgrad_f32(cg.NHWC, s, d["w32"], d["dy32"], d["dx32"], accumulate=False),
+          "wgrad32": lambda: cg.wgrad_f32(cg.NHWC, s, d["dy32"], d["x32"], d["dw32"], net.ws32)}[op]
     ms = timed(torch, fn, args.steps, args.warmup, torch.cuda.current_stream())
     cg.check_device()
     fl = conv_flops(layers[idx], batch)
@@ -1157,8 +1164,8 @@ def main():
     ap.add_argument("--per-layer", default=None,
                     help="write a per-layer table (forward / input grad / weight grad times) to this JSON file")
     ap.add_argument("--only", default=None,
-                    help="LAYER:OP (e.g. s3b2_conv2:fwd): run just that BF16 op, eagerly, warmup+steps times "
-                         "(for profiler captures)")
+                    help="LAYER:OP (e.g. s3b2_conv2:fwd; fwd32 / dgrad32 / wgrad32 for the FP32 drop-in): run "
+                         "just that op, eagerly, warmup+steps times (for profiler captures)")
     ap.add_argument("--workload", default="resnet50", choices=["resnet50", "grouped", "vgg16", "forms"],
                     help="resnet50: the headline fwd+bwd step; grouped: uneven convolutions in one launch")
     ap.add_argument("--group-n", type=int, default=256)
