@@ -49,6 +49,18 @@ constexpr size_t S_SMEM_BYTES = sizeof(float) * SREGS * NT;
 
 __device__ __forceinline__ bool in_range(int v, int n) { return (unsigned) v < (unsigned) n; }
 
+// Four consecutive outputs of one row: one 16-byte store where the caller knows p is aligned
+// and all four exist, else the ones below `valid`.
+__device__ __forceinline__ void store4(float *p, const float (&v)[4], bool vec, int valid) {
+    if (vec && valid >= 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (j < valid) p[j] = v[j];
+    }
+}
+
 // The forward epilogue, operation by operation as the reference does it
 // (src/im2row_nhwc.c:276-282, src/im2col_nchw.c:422-431); the gamma/beta step is
 // one fused multiply-add, as gcc contracts it in the reference's -Ofast build.
@@ -76,6 +88,7 @@ struct FwdOp {
     ConvGeom g;
     int nchw;        // layout of y
     int xl, wl;      // layout of the x the kernel reads (0 NHWC, 1 NCHW) and of w (0 [K][kn], 1 [kn][K])
+    int ov;          // y NHWC with 16-byte aligned rows of kn % 4 == 0
     const float *w, *x;
     float *y;
     cg_epi e;
@@ -101,6 +114,7 @@ struct FwdOp {
     // Single-tap NHWC: the row's reduction indices are its input pixel's channels, contiguous.
     __device__ bool row_in(const Row &rw) const { return in_range(rw.ix, g.h) && in_range(rw.iy, g.w); }
     __device__ const float *asrc() const { return x; }
+    __device__ const float *bsrc() const { return w; }
     struct Col { long long base; int valid; };
     __device__ Col col(int n) const { return Col{wl ? (long long) n * g.K : (long long) n, n < g.kn}; }
     struct alignas(16) REnt { int delta, ox, oy, bd; };
@@ -140,9 +154,18 @@ struct FwdOp {
     __device__ float s_init(int m, int n) const { return 0.0f; }
     __device__ float s_start(int m, int n) const { return 0.0f; }
     __device__ int zcount(int m, int nz) const { return nz; }
-    __device__ void finish_z(int z, int m, int n, float s) const {
-        if (!ws) return finish(m, n, s);
-        if (m < (int) g.P && n < g.kn) ws[((size_t) z * g.P + m) * g.kn + n] = s;
+    __device__ void finish_z4(int z, int m, int n, const float (&s)[4]) const {
+        if (m >= (int) g.P) return;
+        if (ws) return store4(ws + ((size_t) z * g.P + m) * g.kn + n, s, g.kn % 4 == 0, g.kn - n);
+        if (!ov) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) finish(m, n + j, s[j]);
+            return;
+        }
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = n + j < g.kn ? fwd_epilogue(s[j], n + j, e) : 0.0f;
+        store4(y + (size_t) m * g.kn + n, v, true, g.kn - n);
     }
     __device__ void finish(int m, int n, float s) const {
         if (m >= (int) g.P || n >= g.kn) return;
@@ -169,6 +192,7 @@ struct WgradOp {
     int nchw;
     const float *dy, *x;
     float *ws;   // [nblocks][K][kn]
+    int ov;      // ws 16-byte aligned, kn % 4 == 0
     FastDiv dwo, dho, dkw, dkh;
 
     __host__ __device__ int M() const { return g.K; }
@@ -190,6 +214,7 @@ struct WgradOp {
     __device__ Col col(int n) const {
         return Col{nchw ? (long long) n * g.ho * g.wo : (long long) n, n < g.kn};
     }
+    __device__ const float *bsrc() const { return dy; }
     struct alignas(16) REnt { long long base; int ix, iy; long long bd; long long pad; };
     __device__ REnt rent(int r, int rend) const {
         uint32_t q, oy, ox, bb;
@@ -219,9 +244,8 @@ struct WgradOp {
     }
     __device__ int next_fold(int r, int rend) const { return INT_MAX; }
     __device__ float s_init(int m, int n) const { return 0.0f; }
-    __device__ void finish_z(int z, int m, int n, float s) const {
-        if (m >= g.K || n >= g.kn) return;
-        ws[((size_t) z * g.K + m) * g.kn + n] = s;
+    __device__ void finish_z4(int z, int m, int n, const float (&s)[4]) const {
+        if (m < g.K) store4(ws + ((size_t) z * g.K + m) * g.kn + n, s, ov, g.kn - n);
     }
 };
 
@@ -241,6 +265,7 @@ struct DgradOp {
     int nchw, accumulate;   // layout of dx; dx += result
     int yl;                 // layout of the dy the kernel reads (0 NHWC, 1 NCHW)
     int wl;                 // layout of w: 0 NHWC [c][tap][kn], 1 NCHW [kn][c][tap], 2 packed [tap][kn][c]
+    int ov;                 // dx NHWC with 16-byte aligned rows of c % 4 == 0
     const float *w, *dy;
     float *dx;
     FastDiv dw_, dh_, dkn, dkw, dvs, dhs;
@@ -270,6 +295,7 @@ struct DgradOp {
         return rw.cls == 0 && in_range(rw.ix, g.ho) && in_range(rw.iy, g.wo);
     }
     __device__ const float *asrc() const { return dy; }
+    __device__ const float *bsrc() const { return w; }
     struct Col { long long base; int valid; };
     __device__ Col col(int n) const {
         const long long b = wl == 2 ? n : wl == 1 ? (long long) n * g.kh * g.kw : (long long) n * g.kh * g.kw * g.kn;
@@ -333,9 +359,12 @@ struct DgradOp {
         return dx[out_index(m, n)];
     }
     __device__ int zcount(int m, int nz) const { return nz; }
-    __device__ void finish_z(int z, int m, int n, float s) const {
-        if (!ws) return finish(m, n, s);
-        if (m < M() && n < g.c) ws[((size_t) z * M() + m) * g.c + n] = s;
+    __device__ void finish_z4(int z, int m, int n, const float (&s)[4]) const {
+        if (m >= M()) return;
+        if (ws) return store4(ws + ((size_t) z * M() + m) * g.c + n, s, g.c % 4 == 0, g.c - n);
+        if (ov) return store4(dx + (size_t) m * g.c + n, s, true, g.c - n);
+#pragma unroll
+        for (int j = 0; j < 4; j++) finish(m, n + j, s[j]);
     }
     __device__ void finish(int m, int n, float s) const {
         if (m >= M() || n >= g.c) return;
@@ -362,7 +391,7 @@ struct DgPhase {
 };
 struct DgradPhaseOp {
     ConvGeom g;
-    int nchw, accumulate, yl, wl;   // as in DgradOp
+    int nchw, accumulate, yl, wl, ov;   // as in DgradOp
     const float *w, *dy;
     float *dx;
     FastDiv dkn, dvs, dhs;
@@ -410,6 +439,7 @@ struct DgradPhaseOp {
     }
     __device__ bool row_in(const Row &rw) const { return in_range(rw.ix, g.ho) && in_range(rw.iy, g.wo); }
     __device__ const float *asrc() const { return dy; }
+    __device__ const float *bsrc() const { return w; }
     struct Col { long long base; int valid; };
     __device__ Col col(int n) const {
         const long long b = wl == 2 ? n : wl == 1 ? (long long) n * g.kh * g.kw : (long long) n * g.kh * g.kw * g.kn;
@@ -478,9 +508,15 @@ struct DgradPhaseOp {
         return accumulate && out_index(m, n, o) ? dx[o] : 0.0f;
     }
     __device__ float s_init(int m, int n) const { return ws ? 0.0f : s_start(m, n); }
-    __device__ void finish_z(int z, int m, int n, float s) const {
-        if (!ws) return finish(m, n, s);
-        if (z < zcount(m, 0) && n < g.c) ws[((size_t) z * mpad + m) * g.c + n] = s;
+    __device__ void finish_z4(int z, int m, int n, const float (&s)[4]) const {
+        if (ws) {
+            if (z < zcount(m, 0)) store4(ws + ((size_t) z * mpad + m) * g.c + n, s, g.c % 4 == 0, g.c - n);
+            return;
+        }
+        size_t o;
+        if (ov && out_index(m, n, o)) return store4(dx + o, s, true, g.c - n);
+#pragma unroll
+        for (int j = 0; j < 4; j++) finish(m, n + j, s[j]);
     }
     __device__ void finish(int m, int n, float s) const {
         size_t o;
@@ -505,7 +541,9 @@ using TileTall = Tile<256, 64>;
 // channels of one pixel, so each thread loads whole 4-index quads of its row as 16-byte
 // vectors (two threads cover the 8 indices of a row in a slice) instead of gathering
 // element by element down a column.
-template <class Op, class T, bool VEC>
+// BV (B read from a layout with the tile's columns contiguous, N % 4 == 0, 16-byte aligned):
+// each B row of a slice is loaded as BN/4 16-byte vectors, one per thread.
+template <class Op, class T, bool VEC, bool BV>
 __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
     __shared__ __align__(16) float As[2][BK][T::BM];
     __shared__ __align__(16) float Bs[2][BK][T::BN];
@@ -530,9 +568,11 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
     static_assert(!VEC || 4 * VQ == T::AP, "a thread's A quads cover its A elements");
     const int am = VEC ? tid / TPR : tid % T::BM, ak = tid / T::BM, vq = (tid % TPR) * VQ;
     const int bn = tid % T::BN, bk = tid / T::BN;
+    constexpr int QB = T::BN / 4;   // BV: 16-byte quads per B row of a slice
     const auto arow = op.row(m0 + am);
-    const auto bcol = op.col(n0 + bn);
+    const auto bcol = op.col(n0 + (BV ? 4 * (tid % QB) : bn));
     float ra[T::AP], rb[T::BP];
+    float4 rbv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float *vsrc = nullptr;
     if constexpr (VEC) vsrc = op.row_in(arow) ? op.asrc() + arow.base : nullptr;
 
@@ -589,8 +629,16 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
 #pragma unroll
             for (int i = 0; i < T::AP; i++) ra[i] = op.a(arow, rt[ak + T::AS * i]);
         }
+        if constexpr (BV) {
+            if (tid < BK * QB) {
+                const long long bd = rt[tid / QB].bd;
+                rbv = bcol.valid && bd >= 0 ? __ldg(reinterpret_cast<const float4 *>(op.bsrc() + (bcol.base + bd)))
+                                            : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        } else {
 #pragma unroll
-        for (int i = 0; i < T::BP; i++) rb[i] = op.b(bcol, rt[bk + T::BS * i]);
+            for (int i = 0; i < T::BP; i++) rb[i] = op.b(bcol, rt[bk + T::BS * i]);
+        }
     };
     auto sstore = [&](int buf) {
         if constexpr (VEC) {
@@ -602,8 +650,12 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
 #pragma unroll
             for (int i = 0; i < T::AP; i++) As[buf][ak + T::AS * i][am] = ra[i];
         }
+        if constexpr (BV) {
+            if (tid < BK * QB) *reinterpret_cast<float4 *>(&Bs[buf][tid / QB][4 * (tid % QB)]) = rbv;
+        } else {
 #pragma unroll
-        for (int i = 0; i < T::BP; i++) Bs[buf][bk + T::BS * i][bn] = rb[i];
+            for (int i = 0; i < T::BP; i++) Bs[buf][bk + T::BS * i][bn] = rb[i];
+        }
     };
     auto step = [&](int buf, int kk) {
         const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
@@ -655,9 +707,11 @@ __global__ void __launch_bounds__(NT, 2) fp32_igemm_kernel(const Op op) {
 #pragma unroll
     for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const float s = Ssm[(i * 8 + j) * NT + tid];
-            op.finish_z(z, mrow(i), ncol(j), s);
+        for (int q = 0; q < 2; q++) {   // columns ncol(4q) .. ncol(4q) + 3 are consecutive
+            float v[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) v[j] = Ssm[(i * 8 + q * 4 + j) * NT + tid];
+            op.finish_z4(z, mrow(i), ncol(4 * q), v);
         }
 }
 
@@ -706,36 +760,43 @@ __global__ void wgrad_reduce_kernel(const float *__restrict__ ws, float *__restr
     }
 }
 
-template <class Op, class T, bool VEC>
+template <class Op, class T, bool VEC, bool BV>
 cudaError_t launch_tile(const Op &op, int gz, cudaStream_t st) {
     static bool attr_set = false;  // per template instance; harmless if set twice
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(fp32_igemm_kernel<Op, T, VEC>,
+        cudaError_t e = cudaFuncSetAttribute(fp32_igemm_kernel<Op, T, VEC, BV>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int) S_SMEM_BYTES);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     dim3 grid((op.M() + T::BM - 1) / T::BM, (op.N() + T::BN - 1) / T::BN, gz);
     if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-    fp32_igemm_kernel<Op, T, VEC><<<grid, NT, S_SMEM_BYTES, st>>>(op); cg_note_launch();
+    fp32_igemm_kernel<Op, T, VEC, BV><<<grid, NT, S_SMEM_BYTES, st>>>(op); cg_note_launch();
     return cudaGetLastError();
 }
 
 // 256 x 64 tiles where a 128-wide tile would compute padding columns.
 inline bool tall_tiles(int N) { return N <= 64; }
 
-template <class Op, bool VEC>
+template <class Op, bool VEC, bool BV>
 cudaError_t launch_shape(const Op &op, int gz, cudaStream_t st) {
-    return tall_tiles(op.N()) ? launch_tile<Op, TileTall, VEC>(op, gz, st)
-                              : launch_tile<Op, TileSquare, VEC>(op, gz, st);
+    return tall_tiles(op.N()) ? launch_tile<Op, TileTall, VEC, BV>(op, gz, st)
+                              : launch_tile<Op, TileSquare, VEC, BV>(op, gz, st);
 }
 
+template <class Op, bool VEC>
+cudaError_t launch_bv(const Op &op, int gz, bool bv, cudaStream_t st) {
+    return bv ? launch_shape<Op, VEC, true>(op, gz, st) : launch_shape<Op, VEC, false>(op, gz, st);
+}
+
+// vec: A rows as channel vectors (single-tap NHWC forward / input gradient), taken together
+// with bv (B rows as 16-byte vectors), which the same layouts allow.
 template <class Op>
-cudaError_t launch(const Op &op, int gz, bool vec, cudaStream_t st) {
+cudaError_t launch(const Op &op, int gz, bool vec, bool bv, cudaStream_t st) {
     if constexpr (!std::is_same<Op, WgradOp>::value) {
-        if (vec) return launch_shape<Op, true>(op, gz, st);
+        if (vec && bv) return launch_shape<Op, true, true>(op, gz, st);
     }
-    return launch_shape<Op, false>(op, gz, st);
+    return launch_bv<Op, false>(op, gz, bv, st);
 }
 
 // Gathers add 32-bit offsets within one image and within the weights.
@@ -815,7 +876,7 @@ inline bool aligned16(const void *p) { return ((uintptr_t) p & 15) == 0; }
 // rate at full waves (about 35 TFLOP/s) scaled by the fraction of CTA slots its waves fill,
 // plus the planes' bytes at about 4 TB/s.
 template <class Op>
-cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, cudaStream_t st) {
+cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, bool bv, cudaStream_t st) {
     const int bm = tall_tiles(N) ? TileTall::BM : TileSquare::BM, bn = tall_tiles(N) ? TileTall::BN : TileSquare::BN;
     const long long tiles = (long long) ((M + bm - 1) / bm) * ((N + bn - 1) / bn);
     const int nz = op.segments();
@@ -832,8 +893,8 @@ cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, cudaStream_t st
         const double t_split = flops / (rate * filled((double) tiles * nz)) + 2.0 * (double) bytes / 4e12;
         if (t_split < t_fused) op.ws = scratch(SLOT_SPLIT, bytes, st);
     }
-    if (!op.ws) return launch(op, 1, vec, st);
-    cudaError_t e = launch(op, nz, vec, st);
+    if (!op.ws) return launch(op, 1, vec, bv, st);
+    cudaError_t e = launch(op, nz, vec, bv, st);
     if (e != cudaSuccess) return e;
     const long long total = (long long) M * N;
     const int blocks = (int) std::min<long long>((total + 255) / 256, (long long) sms * 16);
@@ -877,7 +938,9 @@ cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float
         op.w = wt;
         op.wl = 0;
     }
-    return launch_split_or_fused(op, (int) op.g.P, op.g.kn, vec, st);
+    op.ov = !nchw && s.kn % 4 == 0 && aligned16(y);
+    const bool bv = op.wl == 0 && s.kn % 4 == 0 && aligned16(op.w);
+    return launch_split_or_fused(op, (int) op.g.P, op.g.kn, vec, bv, st);
 }
 
 size_t cg_fp32_wgrad_ws_bytes(const cg_shape &s) {
@@ -900,7 +963,8 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     op.dkw = FastDiv(s.kw);
     op.dkh = FastDiv(s.kh);
     const int nblocks = (int) ((op.g.P + KC - 1) / KC);
-    cudaError_t e = launch(op, nblocks, false, st);
+    op.ov = s.kn % 4 == 0 && aligned16(ws);
+    cudaError_t e = launch(op, nblocks, false, !nchw && s.kn % 4 == 0 && aligned16(dy), st);
     if (e != cudaSuccess) return e;
     const long long total = (long long) op.g.K * op.g.kn;
     int blocks = (int) std::min<long long>((total + 255) / 256, 152LL * 16);
@@ -950,7 +1014,9 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     } else if (nchw && taps == 1) {
         op.wl = 2;   // [kn][c] is [tap][kn][c] already
     }
-    if (!phased) return launch_split_or_fused(op, op.M(), op.g.c, vec, st);
+    op.ov = !nchw && s.c % 4 == 0 && aligned16(dx);
+    const bool bv = op.wl == 2 && s.c % 4 == 0 && aligned16(op.w);
+    if (!phased) return launch_split_or_fused(op, op.M(), op.g.c, vec, bv, st);
 
     DgradPhaseOp po;
     po.g = op.g;
@@ -958,6 +1024,7 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     po.accumulate = accumulate;
     po.yl = op.yl;
     po.wl = op.wl;
+    po.ov = op.ov;
     po.w = op.w;
     po.dy = op.dy;
     po.dx = dx;
@@ -991,5 +1058,5 @@ cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const flo
     if (m > INT_MAX / 2) return cudaErrorNotSupported;
     po.ncls = c;
     po.mpad = (int) m;
-    return launch_split_or_fused(po, po.mpad, s.c, vec && taps == 1, st);
+    return launch_split_or_fused(po, po.mpad, s.c, vec && taps == 1, bv, st);
 }
