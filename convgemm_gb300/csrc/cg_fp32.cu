@@ -21,13 +21,12 @@
 // completed KC blocks lives in shared memory (it is touched once per 384
 // reduction steps).
 //
-// Block split: when a convolution's tiles fill less than the GPU (the 14x14 and 7x7
-// layers), the forward and input gradient run one CTA per (tile, reduction segment):
-// each CTA writes the FMA chain of one KC block (input gradient: one KC block of one
-// tap) to a scratch plane, and a second kernel adds the planes in order and applies
-// the epilogue.  The chains start from +0 and so are never -0, hence 0 + chain ==
-// chain and the ordered sum of the planes equals the running sum of the fused form
-// bit for bit.
+// Block split: when a convolution's tiles leave SMs idle or end in a thin last wave,
+// the forward and input gradient run one CTA per (tile, reduction segment): each CTA
+// writes the FMA chain of one KC block (input gradient: one KC block of one tap) to a
+// scratch plane, and a second kernel adds the planes in order to the same start value
+// (0, or dx) and applies the epilogue: the fused form's running sum, the same additions
+// in the same order, so bit for bit the same result.
 #include <climits>
 #include <cmath>
 #include <cstdint>
