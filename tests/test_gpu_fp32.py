@@ -204,3 +204,61 @@ def test_resnet_layer_against_fp64(cglib, oracle_lib):
     idx = rng.choice(y.size, 4000, replace=False)
     want = O.fwd_points_f64(0, g, w, x, idx)
     assert errors(y[idx], want)[0] < FP32_TOL
+
+
+def _offset_copy(a, off):
+    """A device copy of numpy array `a` whose first element sits `off` floats into its allocation
+    (off = 1: 4-byte aligned only, so the kernels' 16-byte vector paths are not taken)."""
+    buf = torch.zeros(a.size + off, dtype=torch.float32, device="cuda")
+    buf[off:] = torch.from_numpy(a).cuda()
+    return buf, buf[off:]
+
+
+@pytest.mark.parametrize("b,h,w,c,kn,k,stride,dil,pad", [
+    (2, 9, 9, 64, 48, 1, 1, 1, 0),     # single tap: 16-byte channel rows of x and dy, 16-byte B rows
+    (2, 9, 7, 6, 10, 1, 1, 1, 0),      # single tap, c and kn not multiples of 4: element paths
+    (2, 11, 10, 20, 36, 3, 2, 1, 1),   # stride 2: four stride phases of the input gradient
+    (1, 13, 12, 8, 12, (3, 3), (3, 2), 2, 2),   # strides 3 x 2 with dilation 2: six phases, uneven taps
+    (2, 10, 10, 32, 64, 1, 2, 1, 0),   # 1x1 stride 2: one phase with the tap, three reached by none
+])
+def test_operand_alignment_and_layout_paths_keep_the_bits(cglib, oracle_lib, b, h, w, c, kn, k, stride, dil, pad):
+    """The FP32 kernels read operands through vector or element paths and through NCHW copies or
+    repacked weights, chosen by alignment, channel counts and layout; none of that changes the
+    arithmetic.  Every operation gives the same bits with 16-byte aligned tensors and with tensors at
+    a 4-byte offset, the forward and weight gradient equal the reference-order port, and the
+    input gradient (strided ones grouped by stride phase) accumulates within FP32 tolerance of it."""
+    kh, kw = (k, k) if isinstance(k, int) else k
+    sv, sh = (stride, stride) if isinstance(stride, int) else stride
+    g = C.geom(b, h, w, c, kn, kh, kw, vpad=pad, hpad=pad, vstr=sv, hstr=sh, vdil=dil, hdil=dil)
+    ho, wo = C.out_hw(g)
+    K = c * kh * kw
+    rng = np.random.default_rng(b * 7 + c * 3 + kn)
+    x = rng.uniform(-1, 1, b * h * w * c).astype(np.float32)
+    wt = rng.standard_normal(K * kn).astype(np.float32)
+    dy = rng.uniform(-1, 1, b * ho * wo * kn).astype(np.float32)
+    dx0 = rng.uniform(-1, 1, b * h * w * c).astype(np.float32)
+    bias = rng.uniform(-.1, .1, kn).astype(np.float32)
+    cg = cglib
+    for layout in (C.NHWC, C.NCHW):
+        nhwc = layout == C.NHWC
+        conv = cg.sconvGemmNHWC if nhwc else cg.sconvGemmNCHW
+        back = cg.sconvGemmNHWC_back if nhwc else cg.sconvGemmNCHW_back
+        dims = (b, h, w, c) if nhwc else (b, c, h, w)
+        geo = (kn, kh, kw, pad, pad, sv, sh, dil, dil)
+        outs = []
+        for off in (0, 1):
+            keep = []
+            dev = lambda a: keep.append(_offset_copy(a, off)) or keep[-1][1]
+            y, dw, dx = dev(np.zeros(b * ho * wo * kn, np.float32)), dev(np.zeros(K * kn, np.float32)), dev(dx0)
+            conv("N", *dims, *geo, dev(wt), dev(x), y, dev(bias), relu=True)
+            conv("T", *dims, *geo, dev(dy), dev(x), dw)
+            back(*dims, kn, kh, kw, sv, sh, pad, pad, dil, dil, dev(wt), dev(dy), dx)
+            torch.cuda.synchronize()
+            outs.append([t.cpu().numpy() for t in (y, dw, dx)])
+        for name, a0, a1 in zip(("fwd", "wgrad", "dgrad"), *outs):
+            assert bitexact(a0, a1), (layout, name, "aligned and 4-byte-offset operands differ")
+        inp = {"x": x, "w": wt, "dy": dy, "dx0": dx0, "epi": {"bias": bias, "relu": True}}
+        assert bitexact(outs[0][0], port(oracle_lib, "fwd", layout, g, inp, b * ho * wo * kn)), layout
+        assert bitexact(outs[0][1], port(oracle_lib, "wgrad", layout, g, inp, K * kn)), layout
+        want = port(oracle_lib, "dgrad", layout, g, inp, None)
+        assert errors(outs[0][2], want)[0] <= FP32_TOL, layout
