@@ -188,7 +188,7 @@ struct FwdOp {
 // the row, the pixel part from the reduction-index table.
 struct WgradOp {
     ConvGeom g;
-    int nchw;
+    int xl, yl;  // layout of the x and dy the kernel reads (0 NHWC, 1 NCHW)
     const float *dy, *x;
     float *ws;   // [nblocks][K][kn]
     int ov;      // ws 16-byte aligned, kn % 4 == 0
@@ -205,13 +205,13 @@ struct WgradOp {
         Row rw;
         const int offx = (int) kx * g.vdil;
         rw.oy = (int) ky * g.hdil;
-        rw.delta = nchw ? ((int) c * g.h + offx) * g.w + rw.oy : (offx * g.w + rw.oy) * g.c + (int) c;
+        rw.delta = xl ? ((int) c * g.h + offx) * g.w + rw.oy : (offx * g.w + rw.oy) * g.c + (int) c;
         rw.ox = m < g.K ? offx : -OUT;
         return rw;
     }
     struct Col { long long base; int valid; };
     __device__ Col col(int n) const {
-        return Col{nchw ? (long long) n * g.ho * g.wo : (long long) n, n < g.kn};
+        return Col{yl ? (long long) n * g.ho * g.wo : (long long) n, n < g.kn};
     }
     __device__ const float *bsrc() const { return dy; }
     struct alignas(16) REnt { long long base; int ix, iy; long long bd; long long pad; };
@@ -221,12 +221,12 @@ struct WgradOp {
         dho.divmod(q, bb, ox);
         REnt t;
         const int bix = (int) ox * g.vstr - g.vpad, biy = (int) oy * g.hstr - g.hpad;
-        t.base = nchw ? ((long long) bb * g.c * g.h + bix) * g.w + biy
+        t.base = xl ? ((long long) bb * g.c * g.h + bix) * g.w + biy
                       : (((long long) bb * g.h + bix) * g.w + biy) * g.c;
         t.ix = r < rend ? bix : -OUT;
         t.iy = biy;
         const long long hw = (long long) g.ho * g.wo;
-        t.bd = r < rend ? (nchw ? (long long) bb * g.kn * hw + ((long long) ox * g.wo + oy) : (long long) r * g.kn)
+        t.bd = r < rend ? (yl ? (long long) bb * g.kn * hw + ((long long) ox * g.wo + oy) : (long long) r * g.kn)
                         : -1;
         t.pad = 0;
         return t;
@@ -808,9 +808,9 @@ inline bool offsets_fit(const ConvGeom &g) {
 // Library-owned scratch, one grow-only buffer per (device, stream, purpose): a CUDA graph
 // that captured a buffer keeps using it, so buffers are never freed or reused for another
 // stream.  Purposes: the block split's planes, an operand copy in the kernel's gather layout
-// (activation), a repacked weight tensor.
-enum { SLOT_SPLIT = 0, SLOT_ACT = 1, SLOT_WGT = 2 };
-constexpr size_t SLOT_MAX[3] = {(size_t) 256 << 20, (size_t) 4 << 30, (size_t) 256 << 20};
+// (activation; a second one where a call copies two), a repacked weight tensor.
+enum { SLOT_SPLIT = 0, SLOT_ACT = 1, SLOT_WGT = 2, SLOT_ACT2 = 3 };
+constexpr size_t SLOT_MAX[4] = {(size_t) 256 << 20, (size_t) 4 << 30, (size_t) 256 << 20, (size_t) 4 << 30};
 std::mutex g_scratch_mu;
 std::map<std::tuple<int, cudaStream_t, int>, std::pair<float *, size_t>> g_scratch;
 
@@ -953,7 +953,7 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     WgradOp op;
     op.g = make_geom(s);
     if (!offsets_fit(op.g)) return cudaErrorNotSupported;
-    op.nchw = nchw;
+    op.xl = op.yl = nchw;
     op.dy = dy;
     op.x = x;
     op.ws = ws;
@@ -961,9 +961,22 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
     op.dho = FastDiv(op.g.ho);
     op.dkw = FastDiv(s.kw);
     op.dkh = FastDiv(s.kh);
+    if (nchw) {
+        // NCHW dy strides the tile's columns (output channels) by ho*wo: read an NHWC copy, and
+        // for a single tap, whose rows are input channels, an NHWC copy of x as well
+        if (const float *t = transposed(SLOT_ACT, dy, s.b, s.kn, (long long) op.g.ho * op.g.wo, st)) {
+            op.dy = t;
+            op.yl = 0;
+        }
+        if (s.kh * s.kw == 1)
+            if (const float *t = transposed(SLOT_ACT2, x, s.b, s.c, (long long) s.h * s.w, st)) {
+                op.x = t;
+                op.xl = 0;
+            }
+    }
     const int nblocks = (int) ((op.g.P + KC - 1) / KC);
     op.ov = s.kn % 4 == 0 && aligned16(ws);
-    cudaError_t e = launch(op, nblocks, false, !nchw && s.kn % 4 == 0 && aligned16(dy), st);
+    cudaError_t e = launch(op, nblocks, false, op.yl == 0 && s.kn % 4 == 0 && aligned16(op.dy), st);
     if (e != cudaSuccess) return e;
     const long long total = (long long) op.g.K * op.g.kn;
     int blocks = (int) std::min<long long>((total + 255) / 256, 152LL * 16);
