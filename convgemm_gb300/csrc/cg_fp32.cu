@@ -21,6 +21,14 @@
 // completed KC blocks lives in shared memory (it is touched once per 384
 // reduction steps).
 //
+// Operands are read in the layout where a tile's column (or a B row) is
+// contiguous: k x k NHWC activations through NCHW copies, single-tap NHWC rows
+// as 16-byte channel vectors, weights repacked, NCHW weight-gradient operands
+// through NHWC copies (see the entry points at the end).  Strided input
+// gradients group their rows by stride phase (DgradPhaseOp), so each row runs
+// only the taps that reach it.  None of this changes which products are added
+// to an output, or in which order.
+//
 // Block split: when a convolution's tiles leave SMs idle or end in a thin last wave,
 // the forward and input gradient run one CTA per (tile, reduction segment): each CTA
 // writes the FMA chain of one KC block (input gradient: one KC block of one tap) to a
@@ -35,7 +43,6 @@
 #include <map>
 #include <mutex>
 #include <utility>
-#include <vector>
 #include "cg_common.cuh"
 
 namespace {
