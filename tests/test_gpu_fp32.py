@@ -262,3 +262,36 @@ def test_operand_alignment_and_layout_paths_keep_the_bits(cglib, oracle_lib, b, 
         assert bitexact(outs[0][1], port(oracle_lib, "wgrad", layout, g, inp, K * kn)), layout
         want = port(oracle_lib, "dgrad", layout, g, inp, None)
         assert errors(outs[0][2], want)[0] <= FP32_TOL, layout
+
+
+@pytest.mark.parametrize("layout", ["nhwc", "nchw"])
+def test_capture_without_scratch_reads_caller_tensors_with_same_bits(cglib, layout):
+    """Under stream capture the library allocates nothing.  A call on a capturing stream whose
+    scratch (operand copies, repacked weights, split planes) does not exist yet runs the form that
+    reads the caller's tensors in their own layouts, in one kernel; replaying the graph gives the
+    bits of the eager call, which used the copies."""
+    import convgemm_gb300 as cg
+    lay = cg.NHWC if layout == "nhwc" else cg.NCHW
+    for (b, h, c, kn, k, st) in [(4, 14, 64, 96, 3, 1), (2, 15, 32, 48, 3, 2), (2, 9, 32, 40, 1, 2)]:
+        s = cg.Shape.of(b, h, h, c, kn, k, k, k // 2, k // 2, st, st)
+        gen = torch.Generator(device="cuda").manual_seed(b * 100 + c + kn)
+        x = torch.randn(b * h * h * c, device="cuda", generator=gen)
+        w = torch.randn(c * k * k * kn, device="cuda", generator=gen)
+        dy = torch.randn(b * s.ho * s.wo * kn, device="cuda", generator=gen)
+        bias = torch.randn(kn, device="cuda", generator=gen) * 0.1
+        dx_start = torch.randn(b * h * h * c, device="cuda", generator=gen)
+        y0, y1 = (torch.empty(b * s.ho * s.wo * kn, device="cuda") for _ in range(2))
+        dx0, dx1 = dx_start.clone(), dx_start.clone()
+        cg.fwd_f32(lay, s, w, x, y0, bias=bias, relu=True)
+        cg.dgrad_f32(lay, s, w, dy, dx0, accumulate=True)
+        torch.cuda.synchronize()
+        stream = torch.cuda.Stream()   # no scratch exists for this stream yet
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream, capture_error_mode="relaxed"):
+            cg.fwd_f32(lay, s, w, x, y1, bias=bias, relu=True)
+            cg.dgrad_f32(lay, s, w, dy, dx1, accumulate=True)
+        graph.replay()
+        torch.cuda.synchronize()
+        cg.check_device()
+        assert torch.equal(y0.view(torch.int32), y1.view(torch.int32)), (layout, b, h, c, kn, k, st)
+        assert torch.equal(dx0.view(torch.int32), dx1.view(torch.int32)), (layout, b, h, c, kn, k, st)
