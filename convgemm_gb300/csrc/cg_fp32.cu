@@ -909,6 +909,11 @@ cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, bool bv, cudaSt
     return cudaGetLastError();
 }
 
+// A call's launches (operand copies, the kernel, the plane reduction) are enqueued under one
+// lock: the copies live in per-stream scratch, so two host threads enqueueing on the same
+// stream must not interleave one call's copy between another call's copy and its kernel.
+std::mutex g_call_mu;
+
 }  // namespace
 
 // Operand layouts the kernel reads (the arithmetic and its order do not depend on them):
@@ -918,6 +923,7 @@ cudaError_t launch_split_or_fused(Op op, int M, int N, bool vec, bool bv, cudaSt
 // its weights as [K][kn] (a row of B contiguous).
 cudaError_t cg_fp32_fwd(int nchw, const cg_shape &s, const float *w, const float *x, float *y,
                         const cg_epi &e, cudaStream_t st) {
+    std::lock_guard<std::mutex> call_lock(g_call_mu);
     FwdOp op;
     op.g = make_geom(s);
     if (!offsets_fit(op.g)) return cudaErrorNotSupported;
@@ -957,6 +963,7 @@ size_t cg_fp32_wgrad_ws_bytes(const cg_shape &s) {
 
 cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const float *x, float *dw, float *ws,
                           cudaStream_t st) {
+    std::lock_guard<std::mutex> call_lock(g_call_mu);
     WgradOp op;
     op.g = make_geom(s);
     if (!offsets_fit(op.g)) return cudaErrorNotSupported;
@@ -996,6 +1003,7 @@ cudaError_t cg_fp32_wgrad(int nchw, const cg_shape &s, const float *dy, const fl
 // [tap][kn][c] (a row of B, consecutive input channels at one (tap, output channel), contiguous).
 cudaError_t cg_fp32_dgrad(int nchw, const cg_shape &s, const float *w, const float *dy, float *dx, int accumulate,
                           cudaStream_t st) {
+    std::lock_guard<std::mutex> call_lock(g_call_mu);
     DgradOp op;
     op.g = make_geom(s);
     if (!offsets_fit(op.g)) return cudaErrorNotSupported;
